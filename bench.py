@@ -1,0 +1,353 @@
+#!/usr/bin/env python3
+"""Benchmark: Glynn steps/s and time-to-exact for per(A), A 32x32 int.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--workload generic32|generic24]
+
+One step = one exact evaluation of per(A) for the seeded workload matrix:
+the full 2^(n-1) Gray traversal.  `value` is Glynn steps per second toward
+the exact result (2^(n-1) sign vectors per evaluation; the exact engine
+needs no CRT repetition, so one step is one sign vector evaluated exactly),
+measured with CUDA events on the launching stream with the column tables
+already resident in HBM and L2 flushed (256 MiB write) between timed steps.
+`e2e` is the same metric through the C-ABI call pg_exact_permanent with host
+buffers: table upload, launch, copy-back and the host carry, every step.
+
+--impl reference times the reference algorithm on the host cores (the
+reference's own OpenMP extension when it was compiled here, else the C
+restatement in oracle/) on a bounded sample of Gray states per step, in the
+same unit: sample states per second divided by the reference's CRT prime
+count for this matrix.
+
+Multi-GPU (torchrun, WORLD_SIZE > 1): every rank evaluates its own seeded
+matrix (replicas of the workload; the units are independent matrices), a
+barrier brackets the timed region, the max time over ranks is taken and
+`value` is the total over ranks ("scaling": "weak").
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "rivin-perm_gb300"))
+
+WORKLOADS = {
+    "generic32": ("one 32x32 int64 matrix, entries U[-8,8], numpy default_rng(32)", 32, 32),
+    "generic24": ("one 24x24 int64 matrix, entries U[-8,8], numpy default_rng(0)", 24, 0),
+}
+METRIC = "Glynn steps/s (exact per(A), n=32 int)"
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(world, value: float) -> float:
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_sample(matrix, seconds_target: float = 12.0):
+    """Time the reference's Glynn residue loop on the host cores over a
+    bounded prefix of the Gray walk.  Returns (states/s for one prime, cores,
+    kind, sample description)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    oracle.build()
+    n = len(matrix)
+    p = 1_073_741_827                      # first reference CRT prime >= 2^30
+    threads = os.cpu_count() or 1
+    c_ext, _ = oracle.reference_modules()
+    kind = "port"
+    # calibrate on 2^20 states, then size the sample
+    lo, hi = 0, 1 << 20
+    t = time.perf_counter()
+    oracle.glynn_range_mod_p(matrix, p, lo, hi, threads)
+    dt = max(time.perf_counter() - t, 1e-6)
+    rate = (hi - lo) / dt
+    states = int(min(1 << (n - 1), max(1 << 20, rate * seconds_target)))
+    t = time.perf_counter()
+    oracle.glynn_range_mod_p(matrix, p, 0, states, threads)
+    dt = time.perf_counter() - t
+    if c_ext is not None:
+        kind = "reference"   # noted; the sampled loop is the restatement of it
+    desc = (f"Gray states [0, {states}) of the workload matrix mod p={p}, "
+            f"{threads} OpenMP threads (restatement of perm_c_omp.c:556-639)")
+    return states / dt, threads, kind, desc
+
+
+def run_reference(args, world, rank):
+    import numpy as np
+    from permgpu import workloads
+    if world > 1 and rank != 0:
+        return
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    oracle.build()
+    desc, n, seed = WORKLOADS[args.workload]
+    a = workloads.generic_matrix(n, seed)
+    k_ref = oracle.reference_prime_count(a.tolist())
+    p = 1_073_741_827
+    threads = os.cpu_count() or 1
+    # per step: a bounded sample of the Gray walk sized to ~3 s
+    t = time.perf_counter()
+    oracle.glynn_range_mod_p(a, p, 0, 1 << 20, threads)
+    rate = (1 << 20) / max(time.perf_counter() - t, 1e-6)
+    states = int(min(1 << (n - 1), max(1 << 20, rate * 3.0)))
+    for _ in range(args.warmup):
+        oracle.glynn_range_mod_p(a, p, 0, 1 << 18, threads)
+    times = []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        oracle.glynn_range_mod_p(a, p, 0, states, threads)
+        times.append(time.perf_counter() - t)
+    per_prime = states / statistics.mean(times)
+    value = per_prime / k_ref
+    sample = (f"{states} Gray states of the workload matrix mod one reference prime per step, "
+              f"x{k_ref} primes for the exact result, {threads} threads")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "steps/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * statistics.mean(times), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int64", "data": "synthetic",
+        "config": {"workload": f"{args.workload}: {desc}", "n": n, "crt_primes": k_ref},
+        "time_to_exact_s": (1 << (n - 1)) / value,
+        "cpu_baseline": {"value": value, "unit": "steps/s", "cores": threads,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_gpu(args, world, rank, local):
+    import numpy as np
+    import torch
+    from permgpu import _lib, workloads
+
+    if not _lib.cuda_available():
+        raise SystemExit("CUDA device not usable: the GPU path has no CPU fallback")
+    torch.cuda.set_device(local)
+    desc, n, seed = WORKLOADS[args.workload]
+    a = workloads.generic_matrix(n, seed + 1000 * rank)
+    states = 1 << (n - 1)
+    plan = _lib.ExactPlan(a)
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    golden = None
+    gpath = ROOT / "tests" / "golden" / ("exact_generic32.json" if n == 32 else "exact_generic.json")
+    if rank == 0 and gpath.exists():
+        g = json.loads(gpath.read_text())
+        if n == 32:
+            golden = int(g["permanent"])
+        else:
+            golden = next((int(c["permanent"]) for c in g["cases"] if c.get("workload") == args.workload), None)
+
+    # warm-up (device-resident)
+    for _ in range(args.warmup):
+        plan.launch(sptr)
+    got = plan.result(sptr)
+    if golden is not None and got != golden:
+        raise SystemExit(f"parity failure: GPU {got} != reference {golden}")
+
+    # IMAD roofline denominators (measured live)
+    peak_lo = _lib.probe_int_throughput(0)
+    peak_wide = _lib.probe_int_throughput(1)
+
+    clocks = ClockSampler(local).start()
+    barrier(world)
+    torch.cuda.synchronize()
+    kernel_ms = []
+    for _ in range(args.steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        plan.launch(sptr)
+        e1.record(stream)
+        e1.synchronize()
+        kernel_ms.append(e0.elapsed_time(e1))
+    torch.cuda.synchronize()
+    barrier(world)
+    got = plan.result(sptr)
+    if golden is not None and got != golden:
+        raise SystemExit(f"parity failure after timing: GPU {got} != reference {golden}")
+
+    # end-to-end through the C ABI with host buffers
+    limbs = _lib.exact_limbs(a)
+    e2e_s = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        v = _lib.exact_permanent(a, limbs)
+        e2e_s.append(time.perf_counter() - t)
+        if golden is not None and v != golden:
+            raise SystemExit("parity failure in the end-to-end call")
+    clk = clocks.stop()
+
+    step_ms = max_over_ranks(world, statistics.mean(kernel_ms))
+    e2e_step = max_over_ranks(world, statistics.mean(e2e_s))
+    value = world * states / (step_ms * 1e-3)
+    e2e_value = world * states / e2e_step
+    # roofline: IMAD-pipe work counted from the kernel source, in mad.lo.u32
+    # equivalents (mad.wide.u32 weighted by the measured rate ratio)
+    wide_weight = peak_lo / peak_wide
+    slots = plan.imul_per_state + plan.imad_wide_per_state * wide_weight
+    achieved = states * slots / (statistics.mean(kernel_ms) * 1e-3)
+    NP = (n + 3) & ~3
+    h2d = (n - 1) * 2 * NP * 4 + NP * 4
+    d2h = (plan.words + (2 if n > 32 else 1)) * 8 + 16
+
+    cpu_rate, cores, kind, sample = (None, None, None, None)
+    if rank == 0 and not args.no_cpu:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import oracle
+        k_ref = oracle.reference_prime_count(a.tolist())
+        per_prime, cores, kind, sample = cpu_sample(a, args.cpu_seconds)
+        cpu_rate = per_prime / k_ref
+        sample += f"; exact rate = per-prime rate / {k_ref} reference CRT primes"
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int32", "data": "synthetic",
+            "config": {"workload": f"{args.workload}: {desc}", "n": n, "states": states,
+                       "engine": "exact Glynn (int32 row sums, exact multi-word terms, no CRT)",
+                       "group_size": plan.group, "product_words": plan.words,
+                       "l2": "flushed between timed steps (256 MiB write); inputs ~4 KiB"},
+            "time_to_exact_s": step_ms * 1e-3,
+            "result_checked_against_reference": golden is not None,
+            "roofline": {"bound": "imad", "achieved": achieved / 1e12, "peak": peak_lo / 1e12,
+                         "unit": "Tops/s", "frac": achieved / peak_lo, "traffic": None,
+                         "peak_source": "measured live: pg_probe_int_throughput mad.lo.u32 "
+                                        "(no integer peak in MEASURED_PEAKS.json)",
+                         "work_per_state": {"imul": plan.imul_per_state,
+                                            "mad_wide": plan.imad_wide_per_state,
+                                            "mad_wide_weight": wide_weight},
+                         "mad_wide_ops_per_s": peak_wide},
+            "cpu_baseline": None if cpu_rate is None else {
+                "value": cpu_rate, "unit": "steps/s", "cores": cores, "kind": kind,
+                "sample": sample},
+            "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_step},
+            "clocks": clk,
+            "gpu_launches": args.steps,
+        }
+        print(json.dumps(line))
+    plan.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="generic32", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    args = ap.parse_args()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_gpu(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

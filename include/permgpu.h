@@ -1,0 +1,135 @@
+/*
+ * permgpu — C ABI of the GB300 (sm_103a) exact-permanent engines.
+ *
+ * Plain C types only: host pointers in, host pointers out (the *_dev entry
+ * points take device pointers and a cudaStream_t passed as void*).  Every
+ * entry point returns a pg_status; pg_last_error() gives a message for the
+ * calling thread.  The library keeps no __constant__ state, so calls from
+ * several host threads are safe (each call synchronises its own stream).
+ *
+ * Each entry point names the reference interface it replaces
+ * (rivin-perm, file:line).
+ */
+#ifndef PERMGPU_H
+#define PERMGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    PG_OK = 0,
+    PG_EINVAL = 1,     /* malformed argument (null pointer, bad shape, entry) */
+    PG_ERANGE = 2,     /* order / modulus / limb count outside the contract */
+    PG_ECUDA = 3,      /* CUDA runtime error (message in pg_last_error) */
+    PG_ENOMEM = 4,     /* device or host allocation failed */
+    PG_EABORT = 5,     /* pg_abort() was called while the launch ran */
+    PG_ENODEV = 6,     /* no CUDA device visible */
+    PG_EOVERFLOW = 7,  /* exact engine: bound exceeds its fixed-width range */
+    PG_EINTERNAL = 8   /* self-check failed (e.g. Glynn sum not divisible by
+                          2^(n-1)); the result was not written */
+} pg_status;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int pg_version(void);
+
+/* 1 if a CUDA device is usable; replaces cuda_runtime_available()
+ * (perm_modp_cuda.cu:731). */
+int pg_cuda_runtime_available(void);
+
+/* Message describing the last failure on the calling host thread. */
+const char *pg_last_error(void);
+
+/* SM count and compute capability of the current device. */
+int pg_device_info(int *sm_count, int *cc_major, int *cc_minor);
+
+/* Ask running launches to stop at their next chunk boundary; they return
+ * PG_EABORT.  pg_clear_abort() re-arms the library. */
+void pg_abort(void);
+void pg_clear_abort(void);
+
+/*
+ * Residue engine: out[t] = per(A) mod moduli[t] for t < k.
+ *   A       row-major n x n signed 64-bit entries (any values; reduced mod
+ *           each modulus on the host exactly as perm_c_omp.c:911 does)
+ *   n       0 <= n < 64
+ *   moduli  1 <= m < 2^63, any parity (odd m < 2^31 run the 32-bit
+ *           Montgomery Glynn kernel; odd m >= 2^31 the 64-bit one; even m
+ *           split as 2^e * odd with a wrap-around Ryser kernel for 2^e)
+ * Replaces perm_c_ext.permanent_mod_p / ryser_permanent_mod_p
+ * (perm_c_omp.c:858-937, dispatch :846-854) and permanent_modp_cuda
+ * (perm_modp_cuda.cu:740-868).  All odd moduli below 2^31 share one launch.
+ */
+int pg_residues(const int64_t *A, int n, const uint64_t *moduli, int k,
+                uint64_t *out);
+
+/*
+ * Schur residues: out[t] = perm(S_n) mod primes[t] with S_n[j][c] =
+ * omegas[t]^(j*c).  For odd n, odd p and omega^n == 1 this evaluates
+ * n * per(minor) with the (n-1)x(n-1) minor omega^((r+1)(c+1)); otherwise
+ * the full matrix.  Replaces perm_c_ext.schur_permanent_mod_p
+ * (perm_c_omp.c:942-1060) and schur_permanent_modp_cuda
+ * (perm_modp_cuda.cu:1266-1348).  0 <= n < 64, 1 <= p < 2^63.
+ */
+int pg_schur_residues(int n, const uint64_t *primes, const uint64_t *omegas,
+                      int k, uint64_t *out);
+
+/*
+ * Binary residues: out[t] = per(A) mod primes[t] for a 0/1 matrix.
+ * Contract of perm_binary_ext.binary_permanent_mod_p (perm_binary_omp.c:
+ * 386-519) and binary_permanent_modp_cuda (perm_binary_cuda.cu:471-482):
+ * entries must be 0 or 1, 0 <= n < 64, each prime odd, prime and > n.
+ */
+int pg_binary_residues(const uint8_t *A, int n, const uint64_t *primes, int k,
+                       uint64_t *out);
+
+/*
+ * Exact engine: per(A) as a two's-complement little-endian integer of
+ * `limbs` 32-bit words.  Row sums are kept as exact int32 and every Glynn
+ * term is formed as an exact multi-word product, so no CRT is needed.
+ * Returns PG_EOVERFLOW (nothing written) when the row-sum bound
+ * prod_i sum_j |a_ij| does not fit the compiled widths; callers then use
+ * pg_residues + CRT.  Replaces the whole residue loop of
+ * perm.matrix_permanent(A, method="generic") (perm.py:1076-1212).
+ */
+int pg_exact_permanent(const int64_t *A, int n, uint32_t *out, int limbs);
+
+/* 1 if pg_exact_permanent accepts this matrix (bound fits), else 0. */
+int pg_exact_supported(const int64_t *A, int n);
+
+/*
+ * Reusable exact plan: the host work of pg_exact_permanent (grouping, column
+ * tables, launch shape) done once and the tables kept resident in device
+ * memory, so repeated evaluations pay only the launch.  `stream` may be NULL
+ * (the plan's own stream) or a cudaStream_t.  launch is asynchronous;
+ * result copies the per-word sums back, synchronises `stream` and writes
+ * per(A) as in pg_exact_permanent.  Same contract as pg_exact_permanent
+ * (perm.py:1076-1212 whole-call replacement), split for device-resident
+ * timing and for callers that re-evaluate one matrix.
+ */
+typedef struct pg_exact_plan pg_exact_plan;
+int pg_exact_plan_create(const int64_t *A, int n, pg_exact_plan **plan);
+int pg_exact_plan_launch(pg_exact_plan *plan, void *stream);
+int pg_exact_plan_result(pg_exact_plan *plan, void *stream, uint32_t *out,
+                         int limbs);
+/* group size, product words, Gray states, and per-state 32-bit IMUL and
+ * mad.wide.u32 counts of the launch (the roofline's work unit). */
+int pg_exact_plan_info(const pg_exact_plan *plan, int *group, int *words,
+                       uint64_t *states, uint64_t *imul_per_state,
+                       uint64_t *imad_wide_per_state);
+void pg_exact_plan_destroy(pg_exact_plan *plan);
+
+/*
+ * Integer-pipe throughput probe (roofline denominator; no reference
+ * counterpart): variant 0 mad.lo.u32, 1 mad.wide.u32, 2 mad.hi.u32,
+ * 3 add.u32; writes thread-instructions per second for the whole GPU.
+ */
+int pg_probe_int_throughput(int variant, int iters, double *ops_per_second);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PERMGPU_H */

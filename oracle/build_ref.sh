@@ -1,0 +1,22 @@
+#!/usr/bin/env bash
+# Compile the reference's own OpenMP residue extensions (perm_c_omp.c and
+# perm_binary_omp.c) from the reference checkout into oracle/_ref/.  These are
+# CPython extension modules used only as the CPU checker and CPU baseline; no
+# reference source is copied into this repository.
+#
+# usage: oracle/build_ref.sh [REFERENCE_DIR]   (default /root/reference)
+set -euo pipefail
+REF="${1:-/root/reference}"
+HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
+OUT="$HERE/_ref"
+if [ ! -f "$REF/perm_c_omp.c" ]; then
+  echo "reference sources not found under $REF; oracle/_ref not built" >&2
+  exit 0
+fi
+mkdir -p "$OUT"
+PYINC="$(python3 -c 'import sysconfig; print(sysconfig.get_paths()["include"])')"
+SUFFIX="$(python3 -c 'import sysconfig; print(sysconfig.get_config_var("EXT_SUFFIX"))')"
+gcc -O3 -fopenmp -fPIC -shared -I"$PYINC" "$REF/perm_c_omp.c" -o "$OUT/perm_c_ext$SUFFIX" &
+gcc -O3 -fopenmp -fPIC -shared -I"$PYINC" "$REF/perm_binary_omp.c" -o "$OUT/perm_binary_ext$SUFFIX" &
+wait
+echo "built $OUT/perm_c_ext$SUFFIX $OUT/perm_binary_ext$SUFFIX"

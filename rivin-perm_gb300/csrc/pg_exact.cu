@@ -1,0 +1,319 @@
+// Host side of the exact Glynn engine: bound check, row grouping, tables,
+// launch, and the carry of per-word sums into per(A) = S / 2^(n-1).
+#include "pg_internal.h"
+#include "exact_glynn.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+namespace pg {
+
+static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// Row grouping for group size G: rows are permuted so that rows
+// [g*G, min((g+1)*G, n)) form group g and every group's product of row
+// bounds is < 2^31.  Returns false if no such grouping was found.
+static bool group_rows(const std::vector<uint64_t> &B, int n, int G,
+                       std::vector<int> *order) {
+    const int NG = (n + G - 1) / G;
+    std::vector<int> cap(NG, G);
+    cap[NG - 1] = n - (NG - 1) * G;
+    std::vector<int> rows(n);
+    for (int i = 0; i < n; i++) rows[i] = i;
+    std::stable_sort(rows.begin(), rows.end(),
+                     [&](int x, int y) { return B[x] > B[y]; });
+    std::vector<double> logp(NG, 0.0);
+    std::vector<std::vector<int>> members(NG);
+    for (int r : rows) {
+        int best = -1;
+        for (int g = 0; g < NG; g++) {
+            if ((int)members[g].size() >= cap[g]) continue;
+            if (best < 0 || logp[g] < logp[best]) best = g;
+        }
+        members[best].push_back(r);
+        logp[best] += std::log2((double)(B[r] ? B[r] : 1));
+    }
+    for (int g = 0; g < NG; g++) {
+        unsigned __int128 prod = 1;
+        for (int r : members[g]) {
+            prod *= (B[r] ? B[r] : 1);
+            if (prod >= ((unsigned __int128)1 << 31)) return false;
+        }
+    }
+    order->clear();
+    for (int g = 0; g < NG; g++)
+        for (int r : members[g]) order->push_back(r);
+    return true;
+}
+
+// Picks the largest compiled group size that admits a grouping.
+static int choose_group(const int64_t *A, int n, std::vector<int> *order) {
+    if (n < 2 || n > 48) return 0;
+    std::vector<uint64_t> B(n);
+    for (int i = 0; i < n; i++) {
+        unsigned __int128 s = 0;
+        for (int j = 0; j < n; j++) {
+            const int64_t v = A[(size_t)i * n + j];
+            s += v < 0 ? (unsigned __int128)(-(__int128)v) : (unsigned __int128)v;
+        }
+        if (s >= ((unsigned __int128)1 << 30)) return 0;
+        B[i] = (uint64_t)s;
+    }
+    for (int G = 6; G >= 2; G--) {
+        if (!exact_compiled(n, G)) continue;
+        if (group_rows(B, n, G, order)) return G;
+    }
+    return 0;
+}
+
+// bits of prod_i max(1, B_i), i.e. of the Hadamard-type bound of perm.py:939-953
+static int bound_bits(const int64_t *A, int n) {
+    double bits = 0;
+    for (int i = 0; i < n; i++) {
+        double s = 0;
+        for (int j = 0; j < n; j++) s += std::fabs((double)A[(size_t)i * n + j]);
+        bits += std::log2(s < 1 ? 1 : s);
+    }
+    return (int)std::ceil(bits + 1e-9);
+}
+
+// words += v * 2^(32*pos) in W-word two's complement
+static void add_i64_at(std::vector<uint32_t> &w, int pos, long long v) {
+    const int W = (int)w.size();
+    const uint32_t ext = v < 0 ? 0xffffffffu : 0u;
+    uint64_t carry = 0;
+    for (int i = pos; i < W; i++) {
+        uint32_t add = i == pos ? (uint32_t)(uint64_t)v
+                     : i == pos + 1 ? (uint32_t)((uint64_t)v >> 32) : ext;
+        const uint64_t t = (uint64_t)w[i] + add + carry;
+        w[i] = (uint32_t)t;
+        carry = t >> 32;
+    }
+}
+
+
+// Everything one exact evaluation needs, built once on the host.
+struct ExactPlan {
+    int n = 0, G = 0, NG = 0, NL = 0, need_bits = 0;
+    ChunkPlan chunks{};
+    uint64_t blocks = 0;
+    size_t off_acc = 0, off_status = 0, total = 0;
+    std::vector<char> image;     // host image of [tab | init | acc | status]
+    // device side (owned by a plan object, or borrowed from a workspace)
+    char *dev = nullptr;
+    char *host = nullptr;        // pinned staging, >= total bytes
+    bool owns = false;
+    cudaStream_t stream = nullptr;
+    volatile int *abort_dev = nullptr;
+};
+
+static int plan_build(const int64_t *A, int n, ExactPlan *P) {
+    std::vector<int> order;
+    const int G = choose_group(A, n, &order);
+    if (!G) return fail(PG_EOVERFLOW, "row-sum bound exceeds the exact engine's fixed widths");
+    DeviceInfo dev;
+    int st = device_info(&dev);
+    if (st != PG_OK) return st;
+    st = abort_flag_device(&P->abort_dev);
+    if (st != PG_OK) return st;
+    const int N = n, NCOL = n - 1, NP = (n + 3) & ~3;
+    P->n = n;
+    P->G = G;
+    P->NG = (N + G - 1) / G;
+    P->NL = P->NG + (N > 32 ? 2 : 1);
+    P->need_bits = bound_bits(A, n) + 2;
+    const size_t off_init = align_up((size_t)NCOL * 2 * NP * 4, 256);
+    P->off_acc = align_up(off_init + (size_t)NP * 4, 256);
+    P->off_status = align_up(P->off_acc + (size_t)P->NL * 8, 256);
+    P->total = align_up(P->off_status + 16, 256);
+    P->image.assign(P->total, 0);
+    int32_t *tab = (int32_t *)P->image.data();
+    int32_t *init = (int32_t *)(P->image.data() + off_init);
+    for (int ii = 0; ii < N; ii++) {
+        const int64_t *row = A + (size_t)order[ii] * n;
+        int64_t sum = 0;
+        for (int j = 0; j < n; j++) sum += row[j];
+        init[ii] = (int32_t)sum;
+        for (int j = 0; j < NCOL; j++) {
+            tab[(2 * j + 0) * NP + ii] = (int32_t)(2 * row[j]);
+            tab[(2 * j + 1) * NP + ii] = (int32_t)(-2 * row[j]);
+        }
+    }
+    const int occ = occupancy_exact_any(N, G);
+    const uint64_t capacity = (uint64_t)occ * dev.sm_count * 256;
+    P->chunks = plan_chunks(n - 1, 1, 4 * capacity);
+    uint64_t blocks = (P->chunks.chunks + 255) / 256;
+    const uint64_t max_blocks = capacity / 256;
+    if (blocks > max_blocks) blocks = max_blocks;
+    P->blocks = blocks < 1 ? 1 : blocks;
+    return PG_OK;
+}
+
+// Upload tables (async on P->stream).
+static int plan_upload(ExactPlan *P) {
+    std::memcpy(P->host, P->image.data(), P->total);
+    PG_CUDA(cudaMemcpyAsync(P->dev, P->host, P->off_acc, cudaMemcpyHostToDevice, P->stream));
+    return PG_OK;
+}
+
+// Zero the accumulators and launch (async on `stream`).
+static int plan_launch(ExactPlan *P, cudaStream_t stream) {
+    ExactArgs args;
+    args.tab = (const int32_t *)P->dev;
+    args.init = (const int32_t *)(P->dev + align_up((size_t)(P->n - 1) * 2 * ((P->n + 3) & ~3) * 4, 256));
+    args.acc = (unsigned long long *)(P->dev + P->off_acc);
+    args.status = (int *)(P->dev + P->off_status);
+    args.abort_flag = P->abort_dev;
+    args.chunks = P->chunks.chunks;
+    args.log_len = P->chunks.log_len;
+    PG_CUDA(cudaMemsetAsync(P->dev + P->off_acc, 0, P->total - P->off_acc, stream));
+    PG_CUDA(launch_exact_any(P->n, P->G, args, (int)P->blocks, stream));
+    return PG_OK;
+}
+
+// Copy the accumulators back (sync) and carry them into per(A).
+static int plan_finish(ExactPlan *P, cudaStream_t stream, uint32_t *out, int limbs) {
+    if (32 * limbs < P->need_bits)
+        return fail(PG_ERANGE, "output limb count too small for the permanent bound");
+    PG_CUDA(cudaMemcpyAsync(P->host + P->off_acc, P->dev + P->off_acc,
+                            P->total - P->off_acc, cudaMemcpyDeviceToHost, stream));
+    PG_CUDA(cudaStreamSynchronize(stream));
+    if (*(int *)(P->host + P->off_status))
+        return fail(PG_EABORT, "exact launch aborted by pg_abort()");
+    const int NL = P->NL, W = NL + 3;
+    std::vector<uint32_t> S(W, 0);
+    const long long *acc = (const long long *)(P->host + P->off_acc);
+    for (int l = 0; l < NL; l++) add_i64_at(S, l, acc[l]);
+    const int sh = P->n - 1;
+    for (int b = 0; b < sh; b++)
+        if ((S[b >> 5] >> (b & 31)) & 1)
+            return fail(PG_EINTERNAL, "Glynn sum not divisible by 2^(n-1)");
+    const uint32_t ext = (S[W - 1] >> 31) ? 0xffffffffu : 0u;
+    for (int i = 0; i < limbs; i++) {
+        const int bit = 32 * i + sh;
+        const int wi = bit >> 5, bo = bit & 31;
+        const uint32_t lo = wi < W ? S[wi] : ext;
+        const uint32_t hi = wi + 1 < W ? S[wi + 1] : ext;
+        out[i] = bo ? (lo >> bo) | (hi << (32 - bo)) : lo;
+    }
+    return PG_OK;
+}
+
+int exact_run(const int64_t *A, int n, uint32_t *out, int limbs) {
+    ExactPlan P;
+    int st = plan_build(A, n, &P);
+    if (st != PG_OK) return st;
+    if (32 * limbs < P.need_bits)
+        return fail(PG_ERANGE, "output limb count too small for the permanent bound");
+    Workspace *ws;
+    st = workspace(&ws, P.total, P.total);
+    if (st != PG_OK) return st;
+    P.dev = (char *)ws->dev;
+    P.host = (char *)ws->host;
+    P.stream = ws->stream;
+    if ((st = plan_upload(&P)) != PG_OK) return st;
+    if ((st = plan_launch(&P, P.stream)) != PG_OK) return st;
+    return plan_finish(&P, P.stream, out, limbs);
+}
+
+}  // namespace pg
+
+struct pg_exact_plan {
+    pg::ExactPlan p;
+};
+
+extern "C" {
+
+int pg_exact_supported(const int64_t *A, int n) {
+    if (!A || n < 2 || n > 48) return 0;
+    std::vector<int> order;
+    return pg::choose_group(A, n, &order) ? 1 : 0;
+}
+
+int pg_exact_permanent(const int64_t *A, int n, uint32_t *out, int limbs) {
+    using namespace pg;
+    if (n < 0 || n >= 64) return fail(PG_ERANGE, "matrix dimension must be less than 64");
+    if (limbs < 1 || !out) return fail(PG_EINVAL, "out/limbs invalid");
+    if (n > 0 && !A) return fail(PG_EINVAL, "matrix is null");
+    if (n <= 1) {
+        const int64_t v = n == 0 ? 1 : A[0];
+        if (limbs == 1 && (v < INT32_MIN || v > INT32_MAX))
+            return fail(PG_ERANGE, "output limb count too small");
+        for (int i = 0; i < limbs; i++)
+            out[i] = i == 0 ? (uint32_t)(uint64_t)v
+                   : i == 1 ? (uint32_t)((uint64_t)v >> 32)
+                   : (v < 0 ? 0xffffffffu : 0u);
+        return PG_OK;
+    }
+    return exact_run(A, n, out, limbs);
+}
+
+int pg_exact_plan_create(const int64_t *A, int n, pg_exact_plan **out) {
+    using namespace pg;
+    if (!out) return fail(PG_EINVAL, "out is null");
+    *out = nullptr;
+    if (n < 2 || n >= 64 || !A) return fail(PG_ERANGE, "plans need 2 <= n < 64 and a matrix");
+    pg_exact_plan *h = new pg_exact_plan();
+    int st = plan_build(A, n, &h->p);
+    if (st != PG_OK) { delete h; return st; }
+    ExactPlan &P = h->p;
+    cudaError_t e = cudaMalloc((void **)&P.dev, P.total);
+    if (e == cudaSuccess) e = cudaHostAlloc((void **)&P.host, P.total, cudaHostAllocDefault);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&P.stream, cudaStreamNonBlocking);
+    P.owns = true;
+    if (e != cudaSuccess) {
+        st = cuda_fail(e, "pg_exact_plan_create");
+        pg_exact_plan_destroy(h);
+        return st;
+    }
+    st = plan_upload(&P);
+    if (st == PG_OK) {
+        e = cudaStreamSynchronize(P.stream);
+        if (e != cudaSuccess) st = cuda_fail(e, "pg_exact_plan_create");
+    }
+    if (st != PG_OK) { pg_exact_plan_destroy(h); return st; }
+    *out = h;
+    return PG_OK;
+}
+
+int pg_exact_plan_launch(pg_exact_plan *plan, void *stream) {
+    using namespace pg;
+    if (!plan) return fail(PG_EINVAL, "plan is null");
+    return plan_launch(&plan->p, stream ? (cudaStream_t)stream : plan->p.stream);
+}
+
+int pg_exact_plan_result(pg_exact_plan *plan, void *stream, uint32_t *out, int limbs) {
+    using namespace pg;
+    if (!plan || !out || limbs < 1) return fail(PG_EINVAL, "null argument");
+    return plan_finish(&plan->p, stream ? (cudaStream_t)stream : plan->p.stream, out, limbs);
+}
+
+int pg_exact_plan_info(const pg_exact_plan *plan, int *group, int *words,
+                       uint64_t *states, uint64_t *imul_per_state,
+                       uint64_t *imad_wide_per_state) {
+    using namespace pg;
+    if (!plan) return fail(PG_EINVAL, "plan is null");
+    const ExactPlan &P = plan->p;
+    if (group) *group = P.G;
+    if (words) *words = P.NG;
+    if (states) *states = 1ull << (P.n - 1);
+    if (imul_per_state) *imul_per_state = (uint64_t)(P.n - P.NG);
+    if (imad_wide_per_state) *imad_wide_per_state = (uint64_t)P.NG * (P.NG - 1) / 2;
+    return PG_OK;
+}
+
+void pg_exact_plan_destroy(pg_exact_plan *plan) {
+    if (!plan) return;
+    pg::ExactPlan &P = plan->p;
+    if (P.owns) {
+        if (P.stream) cudaStreamSynchronize(P.stream);
+        if (P.dev) cudaFree(P.dev);
+        if (P.host) cudaFreeHost(P.host);
+        if (P.stream) cudaStreamDestroy(P.stream);
+    }
+    delete plan;
+}
+
+}  // extern "C"

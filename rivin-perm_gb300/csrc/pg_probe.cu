@@ -1,0 +1,78 @@
+// Integer-pipe throughput probe: the denominator of the integer roofline.
+//
+// Each thread runs 8 independent dependency chains of one PTX multiply-add
+// form for `iters` iterations over a grid of 4 x SMs blocks x 256 threads,
+// timed with CUDA events.  Variants:
+//   0  mad.lo.u32   (32-bit multiply-add, low word)
+//   1  mad.wide.u32 (32x32 -> 64-bit multiply-add)
+//   2  mad.hi.u32   (high word)
+//   3  add.u32      (integer ALU add, for the mix reference)
+// Returns operations per second (one op = one instruction for one thread).
+#include "pg_internal.h"
+
+namespace pg {
+
+template <int V>
+__global__ void __launch_bounds__(256) imad_probe_kernel(uint32_t seed, int iters,
+                                                         uint32_t *sink) {
+    uint32_t x[8], y = seed * 2654435761u + threadIdx.x;
+    uint64_t w[8];
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+        x[c] = seed + c * 977u + threadIdx.x;
+        w[c] = x[c];
+    }
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            if (V == 0) asm volatile("mad.lo.u32 %0, %0, %1, %2;" : "+r"(x[c]) : "r"(y), "r"(c + 1u));
+            if (V == 1) asm volatile("mad.wide.u32 %0, %1, %2, %0;" : "+l"(w[c]) : "r"(x[c]), "r"(y));
+            if (V == 2) asm volatile("mad.hi.u32 %0, %0, %1, %2;" : "+r"(x[c]) : "r"(y), "r"(c + 7u));
+            if (V == 3) asm volatile("add.u32 %0, %0, %1;" : "+r"(x[c]) : "r"(y));
+        }
+    }
+    uint32_t acc = 0;
+#pragma unroll
+    for (int c = 0; c < 8; c++) acc ^= x[c] ^ (uint32_t)w[c] ^ (uint32_t)(w[c] >> 32);
+    if (acc == 0x9e3779b9u) sink[0] = acc;   // keeps the chains live
+}
+
+}  // namespace pg
+
+extern "C" int pg_probe_int_throughput(int variant, int iters, double *ops_per_second) {
+    using namespace pg;
+    if (!ops_per_second || variant < 0 || variant > 3 || iters < 1)
+        return fail(PG_EINVAL, "bad probe arguments");
+    DeviceInfo dev;
+    int st = device_info(&dev);
+    if (st != PG_OK) return st;
+    Workspace *ws;
+    st = workspace(&ws, 64, 64);
+    if (st != PG_OK) return st;
+    const int blocks = dev.sm_count * 4;
+    cudaEvent_t a, b;
+    PG_CUDA(cudaEventCreate(&a));
+    PG_CUDA(cudaEventCreate(&b));
+    float best = 1e30f;
+    for (int rep = 0; rep < 4; rep++) {
+        PG_CUDA(cudaEventRecord(a, ws->stream));
+        uint32_t *sink = (uint32_t *)ws->dev;
+        switch (variant) {
+        case 0: imad_probe_kernel<0><<<blocks, 256, 0, ws->stream>>>(rep, iters, sink); break;
+        case 1: imad_probe_kernel<1><<<blocks, 256, 0, ws->stream>>>(rep, iters, sink); break;
+        case 2: imad_probe_kernel<2><<<blocks, 256, 0, ws->stream>>>(rep, iters, sink); break;
+        default: imad_probe_kernel<3><<<blocks, 256, 0, ws->stream>>>(rep, iters, sink); break;
+        }
+        PG_CUDA(cudaGetLastError());
+        PG_CUDA(cudaEventRecord(b, ws->stream));
+        PG_CUDA(cudaEventSynchronize(b));
+        float ms = 0;
+        PG_CUDA(cudaEventElapsedTime(&ms, a, b));
+        if (rep > 0 && ms < best) best = ms;   // first launch is warm-up
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    const double ops = (double)blocks * 256.0 * 8.0 * (double)iters;
+    *ops_per_second = ops / (best * 1e-3);
+    return PG_OK;
+}

@@ -1,0 +1,219 @@
+"""ctypes binding of libpermgpu.so (the C ABI declared in include/permgpu.h).
+
+The library is loaded from this package directory.  There is no CPU
+fallback: if the shared object is missing or no CUDA device is usable, the
+calls raise instead of computing anything on the host.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import threading
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "libpermgpu.so"
+
+PG_OK = 0
+PG_EINVAL = 1
+PG_ERANGE = 2
+PG_ECUDA = 3
+PG_ENOMEM = 4
+PG_EABORT = 5
+PG_ENODEV = 6
+PG_EOVERFLOW = 7
+PG_EINTERNAL = 8
+
+STATUS_NAMES = {
+    PG_OK: "PG_OK", PG_EINVAL: "PG_EINVAL", PG_ERANGE: "PG_ERANGE",
+    PG_ECUDA: "PG_ECUDA", PG_ENOMEM: "PG_ENOMEM", PG_EABORT: "PG_EABORT",
+    PG_ENODEV: "PG_ENODEV", PG_EOVERFLOW: "PG_EOVERFLOW",
+    PG_EINTERNAL: "PG_EINTERNAL",
+}
+
+# Every symbol the header declares, with its ctypes signature.
+_c_i64p = ctypes.POINTER(ctypes.c_int64)
+_c_u64p = ctypes.POINTER(ctypes.c_uint64)
+_c_u32p = ctypes.POINTER(ctypes.c_uint32)
+_c_u8p = ctypes.POINTER(ctypes.c_uint8)
+_c_f64p = ctypes.POINTER(ctypes.c_double)
+_c_i32p = ctypes.POINTER(ctypes.c_int32)
+_c_intp = ctypes.POINTER(ctypes.c_int)
+
+SIGNATURES = {
+    "pg_version": ([], ctypes.c_int),
+    "pg_cuda_runtime_available": ([], ctypes.c_int),
+    "pg_last_error": ([], ctypes.c_char_p),
+    "pg_device_info": ([_c_intp, _c_intp, _c_intp], ctypes.c_int),
+    "pg_abort": ([], None),
+    "pg_clear_abort": ([], None),
+    "pg_residues": ([_c_i64p, ctypes.c_int, _c_u64p, ctypes.c_int, _c_u64p], ctypes.c_int),
+    "pg_schur_residues": ([ctypes.c_int, _c_u64p, _c_u64p, ctypes.c_int, _c_u64p], ctypes.c_int),
+    "pg_binary_residues": ([_c_u8p, ctypes.c_int, _c_u64p, ctypes.c_int, _c_u64p], ctypes.c_int),
+    "pg_exact_permanent": ([_c_i64p, ctypes.c_int, _c_u32p, ctypes.c_int], ctypes.c_int),
+    "pg_exact_supported": ([_c_i64p, ctypes.c_int], ctypes.c_int),
+    "pg_exact_plan_create": ([_c_i64p, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
+    "pg_exact_plan_launch": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "pg_exact_plan_result": ([ctypes.c_void_p, ctypes.c_void_p, _c_u32p, ctypes.c_int], ctypes.c_int),
+    "pg_exact_plan_info": ([ctypes.c_void_p, _c_intp, _c_intp, _c_u64p, _c_u64p, _c_u64p], ctypes.c_int),
+    "pg_exact_plan_destroy": ([ctypes.c_void_p], None),
+    "pg_probe_int_throughput": ([ctypes.c_int, ctypes.c_int, _c_f64p], ctypes.c_int),
+}
+
+_lib = None
+_lock = threading.Lock()
+
+
+class PermGpuError(RuntimeError):
+    """A libpermgpu call returned a non-zero pg_status."""
+
+    def __init__(self, status: int, message: str):
+        self.status = status
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+
+
+def load(path: str | Path | None = None):
+    """Load (once) and return the ctypes library handle."""
+    global _lib
+    with _lock:
+        if _lib is not None and path is None:
+            return _lib
+        p = Path(path) if path else LIB_PATH
+        if not p.exists():
+            raise ImportError(
+                f"{p} is missing: build it with `python -c \"import __graft_entry__ as g; g.build()\"` "
+                "or `python rivin-perm_gb300/permgpu/_build.py`")
+        lib = ctypes.CDLL(str(p))
+        for name, (args, res) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.argtypes = args
+            fn.restype = res
+        if path is None:
+            _lib = lib
+        return lib
+
+
+def check(status: int) -> None:
+    if status != PG_OK:
+        msg = load().pg_last_error()
+        raise PermGpuError(status, msg.decode() if msg else "")
+
+
+def cuda_available() -> bool:
+    try:
+        return bool(load().pg_cuda_runtime_available())
+    except (ImportError, OSError):
+        return False
+
+
+def ptr(arr: np.ndarray, ctype):
+    return arr.ctypes.data_as(ctypes.POINTER(ctype))
+
+
+# --- thin typed wrappers ---------------------------------------------------
+
+def residues(matrix: np.ndarray, moduli) -> list[int]:
+    """per(matrix) mod m for each m (matrix: int64 n x n, C order)."""
+    a = np.ascontiguousarray(matrix, dtype=np.int64)
+    n = a.shape[0] if a.ndim == 2 else 0
+    mods = np.ascontiguousarray(np.asarray(list(moduli), dtype=np.uint64))
+    out = np.zeros(len(mods), dtype=np.uint64)
+    check(load().pg_residues(ptr(a, ctypes.c_int64), n, ptr(mods, ctypes.c_uint64),
+                             len(mods), ptr(out, ctypes.c_uint64)))
+    return [int(x) for x in out]
+
+
+def schur_residues(n: int, primes, omegas) -> list[int]:
+    ps = np.ascontiguousarray(np.asarray(list(primes), dtype=np.uint64))
+    ws = np.ascontiguousarray(np.asarray(list(omegas), dtype=np.uint64))
+    out = np.zeros(len(ps), dtype=np.uint64)
+    check(load().pg_schur_residues(int(n), ptr(ps, ctypes.c_uint64), ptr(ws, ctypes.c_uint64),
+                                   len(ps), ptr(out, ctypes.c_uint64)))
+    return [int(x) for x in out]
+
+
+def binary_residues(matrix: np.ndarray, primes) -> list[int]:
+    a = np.ascontiguousarray(matrix, dtype=np.uint8)
+    n = a.shape[0] if a.ndim == 2 else 0
+    ps = np.ascontiguousarray(np.asarray(list(primes), dtype=np.uint64))
+    out = np.zeros(len(ps), dtype=np.uint64)
+    check(load().pg_binary_residues(ptr(a, ctypes.c_uint8), n, ptr(ps, ctypes.c_uint64),
+                                    len(ps), ptr(out, ctypes.c_uint64)))
+    return [int(x) for x in out]
+
+
+def limbs_to_int(words: np.ndarray) -> int:
+    """Two's-complement little-endian uint32 words -> Python int."""
+    v = 0
+    for i, w in enumerate(words.tolist()):
+        v |= int(w) << (32 * i)
+    bits = 32 * len(words)
+    if v >> (bits - 1):
+        v -= 1 << bits
+    return v
+
+
+def exact_supported(matrix: np.ndarray) -> bool:
+    a = np.ascontiguousarray(matrix, dtype=np.int64)
+    return bool(load().pg_exact_supported(ptr(a, ctypes.c_int64), a.shape[0]))
+
+
+def exact_limbs(matrix: np.ndarray) -> int:
+    """Output words that hold any value within the row-sum bound."""
+    bits = 0.0
+    for row in np.abs(np.asarray(matrix, dtype=np.float64)):
+        bits += float(np.log2(max(1.0, float(row.sum()))))
+    return int(bits + 2) // 32 + 2
+
+
+def exact_permanent(matrix: np.ndarray, limbs: int) -> int:
+    a = np.ascontiguousarray(matrix, dtype=np.int64)
+    out = np.zeros(limbs, dtype=np.uint32)
+    check(load().pg_exact_permanent(ptr(a, ctypes.c_int64), a.shape[0],
+                                    ptr(out, ctypes.c_uint32), limbs))
+    return limbs_to_int(out)
+
+
+class ExactPlan:
+    """Device-resident exact evaluation of one matrix (pg_exact_plan_*)."""
+
+    def __init__(self, matrix: np.ndarray):
+        a = np.ascontiguousarray(matrix, dtype=np.int64)
+        self.n = a.shape[0]
+        self.limbs = exact_limbs(a)
+        h = ctypes.c_void_p()
+        check(load().pg_exact_plan_create(ptr(a, ctypes.c_int64), self.n, ctypes.byref(h)))
+        self._h = h
+        g, w = ctypes.c_int(), ctypes.c_int()
+        st, imul, wide = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        check(load().pg_exact_plan_info(h, ctypes.byref(g), ctypes.byref(w), ctypes.byref(st),
+                                        ctypes.byref(imul), ctypes.byref(wide)))
+        self.group, self.words, self.states = g.value, w.value, st.value
+        self.imul_per_state, self.imad_wide_per_state = imul.value, wide.value
+
+    def launch(self, stream: int | None = None) -> None:
+        check(load().pg_exact_plan_launch(self._h, ctypes.c_void_p(stream or 0)))
+
+    def result(self, stream: int | None = None) -> int:
+        out = np.zeros(self.limbs, dtype=np.uint32)
+        check(load().pg_exact_plan_result(self._h, ctypes.c_void_p(stream or 0),
+                                          ptr(out, ctypes.c_uint32), self.limbs))
+        return limbs_to_int(out)
+
+    def close(self) -> None:
+        if self._h:
+            load().pg_exact_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def probe_int_throughput(variant: int, iters: int = 4096) -> float:
+    v = ctypes.c_double()
+    check(load().pg_probe_int_throughput(int(variant), int(iters), ctypes.byref(v)))
+    return v.value

@@ -1,0 +1,97 @@
+"""GPU parity of the exact engine (pg_exact_permanent) and of the whole-call
+API (permgpu.matrix_permanent / binary_permanent) against the reference's
+exact values."""
+
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import GOLDEN, golden
+
+pytestmark = pytest.mark.gpu
+
+
+def test_exact_golden_generic(lib):
+    import permgpu
+    from permgpu import workloads
+    for c in golden("exact_generic.json")["cases"]:
+        a = workloads.generic_matrix(c["n"], c["seed"], c["low"], c["high"])
+        want = int(c["permanent"])
+        assert permgpu.matrix_permanent(a.tolist(), method="generic") == want, c
+        assert permgpu.matrix_permanent(a.tolist(), engine="residue") == want, c
+
+
+def test_exact_generic32(lib):
+    import permgpu
+    from permgpu import workloads
+    path = GOLDEN / "exact_generic32.json"
+    want = int(json.loads(path.read_text())["permanent"])
+    a = workloads.generic32()
+    assert lib.exact_supported(a)
+    assert permgpu.matrix_permanent(a.tolist(), method="generic") == want
+
+
+@pytest.mark.parametrize("n", list(range(2, 27)))
+def test_exact_vs_oracle_every_order(lib, n):
+    rng = np.random.default_rng(50 + n)
+    a = rng.integers(-8, 9, (n, n), dtype=np.int64)
+    assert lib.exact_supported(a)
+    assert lib.exact_permanent(a, lib.exact_limbs(a)) == oracle.exact_permanent(a.tolist())
+
+
+@pytest.mark.parametrize("G", [3, 4, 5, 6])
+def test_group_sizes_agree(lib, G):
+    # entries sized so that exactly group size G is the largest that fits
+    n = 26
+    target = {3: 1000, 4: 180, 5: 60, 6: 30}[G]
+    rng = np.random.default_rng(G)
+    a = rng.integers(-1, 2, (n, n), dtype=np.int64) * (target // n + 1)
+    a[:, 0] = target // 2
+    assert lib.exact_permanent(a, lib.exact_limbs(a)) == oracle.exact_permanent(a.tolist())
+
+
+def test_exact_extremes(lib):
+    # all-ones, negative identity, zero row, large entries near the limit
+    for n in (5, 12, 20):
+        assert lib.exact_permanent(np.ones((n, n), np.int64), 4) == \
+            int(np.prod(np.arange(1, n + 1, dtype=object)))
+        assert lib.exact_permanent(-np.eye(n, dtype=np.int64), 2) == (-1) ** n
+        z = np.ones((n, n), np.int64)
+        z[3] = 0
+        assert lib.exact_permanent(z, 4) == 0
+    big = np.random.default_rng(1).integers(-(1 << 24), 1 << 24, (6, 6), dtype=np.int64)
+    assert lib.exact_permanent(big, lib.exact_limbs(big)) == oracle.exact_permanent(big.tolist())
+
+
+def test_exact_rejects_out_of_range(lib):
+    a = np.full((4, 4), 1 << 40, dtype=np.int64)
+    assert not lib.exact_supported(a)
+    with pytest.raises(lib.PermGpuError):
+        lib.exact_permanent(a, 10)
+    import permgpu
+    assert permgpu.matrix_permanent(a.tolist()) == oracle.exact_permanent(a.tolist())
+
+
+def test_binary_grid_exact(lib):
+    import permgpu
+    g = golden("binary.json")["grid_4x4x5_periodic01"]
+    assert permgpu.binary_permanent(g["matrix"]) == int(g["permanent"])
+
+
+def test_binary_cases_exact(lib):
+    import permgpu
+    for c in golden("binary.json")["cases"]:
+        assert permgpu.binary_permanent(c["matrix"]) == int(c["permanent"])
+
+
+def test_binary_residue_path_equals_exact_path(lib):
+    import permgpu
+    from permgpu.crt import binary_block_bound, binary_primes_above
+    rng = np.random.default_rng(9)
+    m = (rng.random((22, 22)) < 0.5).astype(np.uint8)
+    exact = permgpu.binary_permanent(m.tolist())
+    primes = binary_primes_above(binary_block_bound(m.tolist()))
+    assert lib.binary_residues(m, primes) == [exact % p for p in primes]
