@@ -219,8 +219,12 @@ def run_gpu(args, world, rank, local):
     a = workloads.generic_matrix(n, seed + 1000 * rank)
     states = 1 << (n - 1)
     plan = _lib.ExactPlan(a)
-    stream = torch.cuda.current_stream()
+    # A dedicated (non-default) stream: the kernel and the CUDA events that
+    # time it are recorded on this same stream.
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     sptr = stream.cuda_stream
+    assert sptr != 0
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
     golden = None

@@ -1,4 +1,4 @@
-// Instantiations of the exact Glynn kernel (part 1 of 6).
+// Instantiations of the exact Glynn kernel (part 1 of 8).
 #include "exact_glynn.cuh"
 
 namespace pg {
@@ -6,101 +6,101 @@ namespace pg {
 bool exact_dispatch_1(int N, int G, const ExactArgs *args, int blocks,
                        cudaStream_t stream, cudaError_t *err, int *occ) {
     switch (N * 8 + G) {
-    case 26:
-        if (args) *err = launch_exact_glynn<3, 2>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<3, 2>();
+    case 18:
+        if (args) *err = launch_exact_glynn<2, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<2, 2>();
         return true;
-    case 51:
-        if (args) *err = launch_exact_glynn<6, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<6, 3>();
+    case 41:
+        if (args) *err = launch_exact_glynn<5, 1>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<5, 1>();
         return true;
-    case 75:
-        if (args) *err = launch_exact_glynn<9, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<9, 3>();
+    case 57:
+        if (args) *err = launch_exact_glynn<7, 1>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<7, 1>();
         return true;
-    case 99:
-        if (args) *err = launch_exact_glynn<12, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<12, 3>();
+    case 73:
+        if (args) *err = launch_exact_glynn<9, 1>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<9, 1>();
         return true;
-    case 123:
-        if (args) *err = launch_exact_glynn<15, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<15, 3>();
+    case 89:
+        if (args) *err = launch_exact_glynn<11, 1>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<11, 1>();
         return true;
-    case 147:
-        if (args) *err = launch_exact_glynn<18, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<18, 3>();
+    case 105:
+        if (args) *err = launch_exact_glynn<13, 1>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<13, 1>();
         return true;
-    case 171:
-        if (args) *err = launch_exact_glynn<21, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<21, 3>();
+    case 121:
+        if (args) *err = launch_exact_glynn<15, 1>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<15, 1>();
         return true;
-    case 195:
-        if (args) *err = launch_exact_glynn<24, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<24, 3>();
+    case 138:
+        if (args) *err = launch_exact_glynn<17, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<17, 2>();
         return true;
-    case 205:
-        if (args) *err = launch_exact_glynn<25, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<25, 5>();
+    case 156:
+        if (args) *err = launch_exact_glynn<19, 4>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<19, 4>();
         return true;
-    case 219:
-        if (args) *err = launch_exact_glynn<27, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<27, 3>();
+    case 179:
+        if (args) *err = launch_exact_glynn<22, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<22, 3>();
         return true;
-    case 229:
-        if (args) *err = launch_exact_glynn<28, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<28, 5>();
+    case 197:
+        if (args) *err = launch_exact_glynn<24, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<24, 5>();
         return true;
-    case 243:
-        if (args) *err = launch_exact_glynn<30, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<30, 3>();
+    case 211:
+        if (args) *err = launch_exact_glynn<26, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<26, 3>();
         return true;
-    case 253:
-        if (args) *err = launch_exact_glynn<31, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<31, 5>();
+    case 222:
+        if (args) *err = launch_exact_glynn<27, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<27, 6>();
         return true;
-    case 267:
-        if (args) *err = launch_exact_glynn<33, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<33, 3>();
+    case 236:
+        if (args) *err = launch_exact_glynn<29, 4>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<29, 4>();
+        return true;
+    case 250:
+        if (args) *err = launch_exact_glynn<31, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<31, 2>();
+        return true;
+    case 261:
+        if (args) *err = launch_exact_glynn<32, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<32, 5>();
         return true;
     case 277:
         if (args) *err = launch_exact_glynn<34, 5>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<34, 5>();
         return true;
-    case 291:
-        if (args) *err = launch_exact_glynn<36, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<36, 3>();
+    case 293:
+        if (args) *err = launch_exact_glynn<36, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<36, 5>();
         return true;
-    case 301:
-        if (args) *err = launch_exact_glynn<37, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<37, 5>();
-        return true;
-    case 315:
-        if (args) *err = launch_exact_glynn<39, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<39, 3>();
+    case 309:
+        if (args) *err = launch_exact_glynn<38, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<38, 5>();
         return true;
     case 325:
         if (args) *err = launch_exact_glynn<40, 5>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<40, 5>();
         return true;
-    case 339:
-        if (args) *err = launch_exact_glynn<42, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<42, 3>();
+    case 341:
+        if (args) *err = launch_exact_glynn<42, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<42, 5>();
         return true;
-    case 349:
-        if (args) *err = launch_exact_glynn<43, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<43, 5>();
-        return true;
-    case 363:
-        if (args) *err = launch_exact_glynn<45, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<45, 3>();
+    case 357:
+        if (args) *err = launch_exact_glynn<44, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<44, 5>();
         return true;
     case 373:
         if (args) *err = launch_exact_glynn<46, 5>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<46, 5>();
         return true;
-    case 387:
-        if (args) *err = launch_exact_glynn<48, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<48, 3>();
+    case 389:
+        if (args) *err = launch_exact_glynn<48, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<48, 5>();
         return true;
     default: return false;
     }

@@ -1,4 +1,4 @@
-// Instantiations of the exact Glynn kernel (part 2 of 6).
+// Instantiations of the exact Glynn kernel (part 2 of 8).
 #include "exact_glynn.cuh"
 
 namespace pg {
@@ -6,101 +6,101 @@ namespace pg {
 bool exact_dispatch_2(int N, int G, const ExactArgs *args, int blocks,
                        cudaStream_t stream, cudaError_t *err, int *occ) {
     switch (N * 8 + G) {
-    case 27:
-        if (args) *err = launch_exact_glynn<3, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<3, 3>();
+    case 25:
+        if (args) *err = launch_exact_glynn<3, 1>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<3, 1>();
         return true;
-    case 52:
-        if (args) *err = launch_exact_glynn<6, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<6, 4>();
+    case 42:
+        if (args) *err = launch_exact_glynn<5, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<5, 2>();
         return true;
-    case 76:
-        if (args) *err = launch_exact_glynn<9, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<9, 4>();
+    case 58:
+        if (args) *err = launch_exact_glynn<7, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<7, 2>();
         return true;
-    case 100:
-        if (args) *err = launch_exact_glynn<12, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<12, 4>();
+    case 74:
+        if (args) *err = launch_exact_glynn<9, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<9, 2>();
         return true;
-    case 124:
-        if (args) *err = launch_exact_glynn<15, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<15, 4>();
+    case 90:
+        if (args) *err = launch_exact_glynn<11, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<11, 2>();
         return true;
-    case 148:
-        if (args) *err = launch_exact_glynn<18, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<18, 4>();
+    case 106:
+        if (args) *err = launch_exact_glynn<13, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<13, 2>();
         return true;
-    case 172:
-        if (args) *err = launch_exact_glynn<21, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<21, 4>();
+    case 122:
+        if (args) *err = launch_exact_glynn<15, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<15, 2>();
         return true;
-    case 196:
-        if (args) *err = launch_exact_glynn<24, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<24, 4>();
+    case 139:
+        if (args) *err = launch_exact_glynn<17, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<17, 3>();
         return true;
-    case 206:
-        if (args) *err = launch_exact_glynn<25, 6>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<25, 6>();
+    case 162:
+        if (args) *err = launch_exact_glynn<20, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<20, 2>();
         return true;
-    case 220:
-        if (args) *err = launch_exact_glynn<27, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<27, 4>();
+    case 180:
+        if (args) *err = launch_exact_glynn<22, 4>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<22, 4>();
         return true;
-    case 230:
-        if (args) *err = launch_exact_glynn<28, 6>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<28, 6>();
+    case 198:
+        if (args) *err = launch_exact_glynn<24, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<24, 6>();
         return true;
-    case 244:
-        if (args) *err = launch_exact_glynn<30, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<30, 4>();
+    case 212:
+        if (args) *err = launch_exact_glynn<26, 4>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<26, 4>();
         return true;
-    case 254:
-        if (args) *err = launch_exact_glynn<31, 6>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<31, 6>();
+    case 226:
+        if (args) *err = launch_exact_glynn<28, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<28, 2>();
         return true;
-    case 268:
-        if (args) *err = launch_exact_glynn<33, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<33, 4>();
+    case 237:
+        if (args) *err = launch_exact_glynn<29, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<29, 5>();
+        return true;
+    case 251:
+        if (args) *err = launch_exact_glynn<31, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<31, 3>();
+        return true;
+    case 262:
+        if (args) *err = launch_exact_glynn<32, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<32, 6>();
         return true;
     case 278:
         if (args) *err = launch_exact_glynn<34, 6>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<34, 6>();
         return true;
-    case 292:
-        if (args) *err = launch_exact_glynn<36, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<36, 4>();
+    case 294:
+        if (args) *err = launch_exact_glynn<36, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<36, 6>();
         return true;
-    case 302:
-        if (args) *err = launch_exact_glynn<37, 6>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<37, 6>();
-        return true;
-    case 316:
-        if (args) *err = launch_exact_glynn<39, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<39, 4>();
+    case 310:
+        if (args) *err = launch_exact_glynn<38, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<38, 6>();
         return true;
     case 326:
         if (args) *err = launch_exact_glynn<40, 6>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<40, 6>();
         return true;
-    case 340:
-        if (args) *err = launch_exact_glynn<42, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<42, 4>();
+    case 342:
+        if (args) *err = launch_exact_glynn<42, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<42, 6>();
         return true;
-    case 350:
-        if (args) *err = launch_exact_glynn<43, 6>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<43, 6>();
-        return true;
-    case 364:
-        if (args) *err = launch_exact_glynn<45, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<45, 4>();
+    case 358:
+        if (args) *err = launch_exact_glynn<44, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<44, 6>();
         return true;
     case 374:
         if (args) *err = launch_exact_glynn<46, 6>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<46, 6>();
         return true;
-    case 388:
-        if (args) *err = launch_exact_glynn<48, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<48, 4>();
+    case 390:
+        if (args) *err = launch_exact_glynn<48, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<48, 6>();
         return true;
     default: return false;
     }

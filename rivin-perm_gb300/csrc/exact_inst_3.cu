@@ -1,4 +1,4 @@
-// Instantiations of the exact Glynn kernel (part 3 of 6).
+// Instantiations of the exact Glynn kernel (part 3 of 8).
 #include "exact_glynn.cuh"
 
 namespace pg {
@@ -6,101 +6,97 @@ namespace pg {
 bool exact_dispatch_3(int N, int G, const ExactArgs *args, int blocks,
                        cudaStream_t stream, cudaError_t *err, int *occ) {
     switch (N * 8 + G) {
-    case 35:
-        if (args) *err = launch_exact_glynn<4, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<4, 3>();
+    case 26:
+        if (args) *err = launch_exact_glynn<3, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<3, 2>();
+        return true;
+    case 43:
+        if (args) *err = launch_exact_glynn<5, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<5, 3>();
         return true;
     case 59:
         if (args) *err = launch_exact_glynn<7, 3>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<7, 3>();
         return true;
-    case 83:
-        if (args) *err = launch_exact_glynn<10, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<10, 3>();
+    case 75:
+        if (args) *err = launch_exact_glynn<9, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<9, 3>();
+        return true;
+    case 91:
+        if (args) *err = launch_exact_glynn<11, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<11, 3>();
         return true;
     case 107:
         if (args) *err = launch_exact_glynn<13, 3>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<13, 3>();
         return true;
-    case 131:
-        if (args) *err = launch_exact_glynn<16, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<16, 3>();
+    case 123:
+        if (args) *err = launch_exact_glynn<15, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<15, 3>();
         return true;
-    case 155:
-        if (args) *err = launch_exact_glynn<19, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<19, 3>();
+    case 140:
+        if (args) *err = launch_exact_glynn<17, 4>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<17, 4>();
         return true;
-    case 179:
-        if (args) *err = launch_exact_glynn<22, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<22, 3>();
+    case 163:
+        if (args) *err = launch_exact_glynn<20, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<20, 3>();
         return true;
-    case 197:
-        if (args) *err = launch_exact_glynn<24, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<24, 5>();
+    case 186:
+        if (args) *err = launch_exact_glynn<23, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<23, 2>();
         return true;
-    case 211:
-        if (args) *err = launch_exact_glynn<26, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<26, 3>();
+    case 202:
+        if (args) *err = launch_exact_glynn<25, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<25, 2>();
         return true;
-    case 221:
-        if (args) *err = launch_exact_glynn<27, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<27, 5>();
+    case 213:
+        if (args) *err = launch_exact_glynn<26, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<26, 5>();
         return true;
-    case 235:
-        if (args) *err = launch_exact_glynn<29, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<29, 3>();
+    case 227:
+        if (args) *err = launch_exact_glynn<28, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<28, 3>();
         return true;
-    case 245:
-        if (args) *err = launch_exact_glynn<30, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<30, 5>();
+    case 238:
+        if (args) *err = launch_exact_glynn<29, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<29, 6>();
         return true;
-    case 259:
-        if (args) *err = launch_exact_glynn<32, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<32, 3>();
+    case 252:
+        if (args) *err = launch_exact_glynn<31, 4>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<31, 4>();
         return true;
-    case 269:
-        if (args) *err = launch_exact_glynn<33, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<33, 5>();
+    case 267:
+        if (args) *err = launch_exact_glynn<33, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<33, 3>();
         return true;
     case 283:
         if (args) *err = launch_exact_glynn<35, 3>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<35, 3>();
         return true;
-    case 293:
-        if (args) *err = launch_exact_glynn<36, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<36, 5>();
+    case 299:
+        if (args) *err = launch_exact_glynn<37, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<37, 3>();
         return true;
-    case 307:
-        if (args) *err = launch_exact_glynn<38, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<38, 3>();
-        return true;
-    case 317:
-        if (args) *err = launch_exact_glynn<39, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<39, 5>();
+    case 315:
+        if (args) *err = launch_exact_glynn<39, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<39, 3>();
         return true;
     case 331:
         if (args) *err = launch_exact_glynn<41, 3>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<41, 3>();
         return true;
-    case 341:
-        if (args) *err = launch_exact_glynn<42, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<42, 5>();
+    case 347:
+        if (args) *err = launch_exact_glynn<43, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<43, 3>();
         return true;
-    case 355:
-        if (args) *err = launch_exact_glynn<44, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<44, 3>();
-        return true;
-    case 365:
-        if (args) *err = launch_exact_glynn<45, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<45, 5>();
+    case 363:
+        if (args) *err = launch_exact_glynn<45, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<45, 3>();
         return true;
     case 379:
         if (args) *err = launch_exact_glynn<47, 3>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<47, 3>();
-        return true;
-    case 389:
-        if (args) *err = launch_exact_glynn<48, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<48, 5>();
         return true;
     default: return false;
     }

@@ -1,4 +1,4 @@
-// Instantiations of the exact Glynn kernel (part 5 of 6).
+// Instantiations of the exact Glynn kernel (part 5 of 8).
 #include "exact_glynn.cuh"
 
 namespace pg {
@@ -6,93 +6,93 @@ namespace pg {
 bool exact_dispatch_5(int N, int G, const ExactArgs *args, int blocks,
                        cudaStream_t stream, cudaError_t *err, int *occ) {
     switch (N * 8 + G) {
-    case 43:
-        if (args) *err = launch_exact_glynn<5, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<5, 3>();
+    case 33:
+        if (args) *err = launch_exact_glynn<4, 1>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<4, 1>();
         return true;
-    case 67:
-        if (args) *err = launch_exact_glynn<8, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<8, 3>();
+    case 49:
+        if (args) *err = launch_exact_glynn<6, 1>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<6, 1>();
         return true;
-    case 91:
-        if (args) *err = launch_exact_glynn<11, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<11, 3>();
+    case 65:
+        if (args) *err = launch_exact_glynn<8, 1>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<8, 1>();
         return true;
-    case 115:
-        if (args) *err = launch_exact_glynn<14, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<14, 3>();
+    case 81:
+        if (args) *err = launch_exact_glynn<10, 1>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<10, 1>();
         return true;
-    case 139:
-        if (args) *err = launch_exact_glynn<17, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<17, 3>();
+    case 97:
+        if (args) *err = launch_exact_glynn<12, 1>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<12, 1>();
         return true;
-    case 163:
-        if (args) *err = launch_exact_glynn<20, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<20, 3>();
+    case 113:
+        if (args) *err = launch_exact_glynn<14, 1>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<14, 1>();
         return true;
-    case 187:
-        if (args) *err = launch_exact_glynn<23, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<23, 3>();
+    case 129:
+        if (args) *err = launch_exact_glynn<16, 1>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<16, 1>();
         return true;
-    case 203:
-        if (args) *err = launch_exact_glynn<25, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<25, 3>();
+    case 147:
+        if (args) *err = launch_exact_glynn<18, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<18, 3>();
         return true;
-    case 213:
-        if (args) *err = launch_exact_glynn<26, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<26, 5>();
+    case 170:
+        if (args) *err = launch_exact_glynn<21, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<21, 2>();
         return true;
-    case 227:
-        if (args) *err = launch_exact_glynn<28, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<28, 3>();
+    case 188:
+        if (args) *err = launch_exact_glynn<23, 4>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<23, 4>();
         return true;
-    case 237:
-        if (args) *err = launch_exact_glynn<29, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<29, 5>();
+    case 204:
+        if (args) *err = launch_exact_glynn<25, 4>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<25, 4>();
         return true;
-    case 251:
-        if (args) *err = launch_exact_glynn<31, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<31, 3>();
+    case 218:
+        if (args) *err = launch_exact_glynn<27, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<27, 2>();
         return true;
-    case 261:
-        if (args) *err = launch_exact_glynn<32, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<32, 5>();
+    case 229:
+        if (args) *err = launch_exact_glynn<28, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<28, 5>();
         return true;
-    case 275:
-        if (args) *err = launch_exact_glynn<34, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<34, 3>();
+    case 243:
+        if (args) *err = launch_exact_glynn<30, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<30, 3>();
+        return true;
+    case 254:
+        if (args) *err = launch_exact_glynn<31, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<31, 6>();
+        return true;
+    case 269:
+        if (args) *err = launch_exact_glynn<33, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<33, 5>();
         return true;
     case 285:
         if (args) *err = launch_exact_glynn<35, 5>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<35, 5>();
         return true;
-    case 299:
-        if (args) *err = launch_exact_glynn<37, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<37, 3>();
+    case 301:
+        if (args) *err = launch_exact_glynn<37, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<37, 5>();
         return true;
-    case 309:
-        if (args) *err = launch_exact_glynn<38, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<38, 5>();
-        return true;
-    case 323:
-        if (args) *err = launch_exact_glynn<40, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<40, 3>();
+    case 317:
+        if (args) *err = launch_exact_glynn<39, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<39, 5>();
         return true;
     case 333:
         if (args) *err = launch_exact_glynn<41, 5>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<41, 5>();
         return true;
-    case 347:
-        if (args) *err = launch_exact_glynn<43, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<43, 3>();
+    case 349:
+        if (args) *err = launch_exact_glynn<43, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<43, 5>();
         return true;
-    case 357:
-        if (args) *err = launch_exact_glynn<44, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<44, 5>();
-        return true;
-    case 371:
-        if (args) *err = launch_exact_glynn<46, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<46, 3>();
+    case 365:
+        if (args) *err = launch_exact_glynn<45, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<45, 5>();
         return true;
     case 381:
         if (args) *err = launch_exact_glynn<47, 5>(*args, blocks, stream);

@@ -61,7 +61,7 @@ static int choose_group(const int64_t *A, int n, std::vector<int> *order) {
         if (s >= ((unsigned __int128)1 << 30)) return 0;
         B[i] = (uint64_t)s;
     }
-    for (int G = 6; G >= 2; G--) {
+    for (int G = 6; G >= 1; G--) {
         if (!exact_compiled(n, G)) continue;
         if (group_rows(B, n, G, order)) return G;
     }

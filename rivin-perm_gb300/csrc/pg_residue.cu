@@ -145,6 +145,14 @@ static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 // per(mats[t]) mod moduli[t] for odd moduli 3 <= m < 2^31, n >= 2.
 static int glynn_m32_batch(const uint64_t *mats, int n, const uint64_t *moduli,
                            int k, uint64_t *out) {
+    if (k > 65535) {   // grid.y limit: split into launches of <= 65535 moduli
+        for (int t0 = 0; t0 < k; t0 += 65535) {
+            const int kk = k - t0 < 65535 ? k - t0 : 65535;
+            int st = glynn_m32_batch(mats + (size_t)t0 * n * n, n, moduli + t0, kk, out + t0);
+            if (st != PG_OK) return st;
+        }
+        return PG_OK;
+    }
     DeviceInfo dev;
     int st = device_info(&dev);
     if (st != PG_OK) return st;
