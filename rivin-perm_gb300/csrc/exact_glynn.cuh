@@ -67,14 +67,18 @@ exact_glynn_kernel(ExactArgs a) {
     bool aborted = false;
     const uint32_t Q = (1u << a.log_len) >> 1;
 
-    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-         c < a.chunks; c += (uint64_t)gridDim.x * blockDim.x) {
-        if (*a.abort_flag) { aborted = true; break; }
-        const uint64_t start = c << a.log_len;
-        const uint64_t gstart = start ^ (start >> 1);
-        const uint32_t hib = (uint32_t)(c & 1) << a.log_len;
+    // Each thread walks one contiguous, balanced range of chunks
+    // [c_begin, c_end): the row sums are initialised once, and crossing a
+    // chunk boundary is an ordinary Gray step (column log_len + ctz(c)).
+    const uint64_t T = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t c_begin = tid * a.chunks / T;
+    const uint64_t c_end = (tid + 1) * a.chunks / T;
 
-        int32_t s[N];
+    int32_t s[N];
+    if (c_begin < c_end) {
+        const uint64_t start = c_begin << a.log_len;
+        const uint64_t gstart = start ^ (start >> 1);
 #pragma unroll
         for (int i = 0; i < N; i++) s[i] = a.init[i];
         for (int j = 0; j < NCOL; j++) {
@@ -84,20 +88,31 @@ exact_glynn_kernel(ExactArgs a) {
                 for (int i = 0; i < N; i++) s[i] += col[i];
             }
         }
+    }
 
+    for (uint64_t c = c_begin; c < c_end; c++) {
+        if (((c - c_begin) & 255) == 0 && *a.abort_flag) { aborted = true; break; }
+        const uint32_t hib = (uint32_t)(c & 1) << a.log_len;
         for (uint32_t q = 0; q < Q; q++) {
             const uint32_t g32 = (q << 1) | hib;
 #pragma unroll
             for (int r = 0; r < 2; r++) {
-                if (r != 0 || q != 0) {
-                    int j, sub;
-                    if (r != 0) {
-                        j = 0;
-                        sub = ((g32 >> 1) & 1) == 0;
-                    } else {
-                        j = __ffs(q);  // ctz(q) + 1
-                        sub = ((g32 >> (j + 1)) & 1) == 0;
-                    }
+                bool step = true;
+                int j, sub;
+                if (r != 0) {
+                    j = 0;
+                    sub = ((g32 >> 1) & 1) == 0;
+                } else if (q != 0) {
+                    j = __ffs(q);  // ctz(q) + 1
+                    sub = ((g32 >> (j + 1)) & 1) == 0;
+                } else {
+                    // chunk boundary g = c * 2^log_len (lanes may differ here)
+                    step = c != c_begin;
+                    const int jc = __ffsll((long long)c) - 1;
+                    j = a.log_len + jc;
+                    sub = ((c >> (jc + 1)) & 1) == 0;
+                }
+                if (step) {
                     const int4 *col =
                         reinterpret_cast<const int4 *>(tab + (2 * j + sub) * NP);
 #pragma unroll
@@ -109,8 +124,10 @@ exact_glynn_kernel(ExactArgs a) {
                         if (4 * v + 3 < N) s[4 * v + 3] += d.w;
                     }
                 }
-                // exact group products (|x| < 2^31 by the host's grouping)
-                uint32_t negx = (uint32_t)r;   // Glynn sign (-1)^g, g = start + 2q + r
+                // exact group products (|x| < 2^31 by the host's grouping);
+                // the term's sign is the XOR of the group signs and the
+                // Glynn sign (-1)^g = (-1)^r (chunks start at even states)
+                uint32_t sx = (uint32_t)r << 31;
                 uint32_t mag[NG];
 #pragma unroll
                 for (int g = 0; g < NG; g++) {
@@ -118,9 +135,10 @@ exact_glynn_kernel(ExactArgs a) {
 #pragma unroll
                     for (int t = 1; t < G; t++)
                         if (g * G + t < N) x *= s[g * G + t];
-                    negx ^= (uint32_t)x >> 31;
-                    mag[g] = (uint32_t)(x < 0 ? -x : x);
+                    sx ^= (uint32_t)x;
+                    mag[g] = (uint32_t)abs(x);
                 }
+                const uint32_t negx = sx >> 31;
                 // magnitude as an NG-word integer: P = prod mag[g]
                 uint32_t P[NG];
                 P[0] = mag[0];

@@ -91,15 +91,17 @@ glynn_m32_kernel(M32Args a) {
     unsigned long long thread_sum = 0;
     bool aborted = false;
 
-    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-         c < a.chunks; c += (uint64_t)gridDim.x * blockDim.x) {
-        if (*a.abort_flag) { aborted = true; break; }
-        const uint64_t start = c << a.log_len;
-        const uint64_t gstart = start ^ (start >> 1);
-        // bits 0..log_len of the global state index g = start + i
-        const uint32_t hib = (uint32_t)(c & 1) << a.log_len;
+    // Contiguous, balanced chunk range per thread (see exact_glynn.cuh):
+    // initialise once, cross chunk boundaries with an ordinary Gray step.
+    const uint64_t T = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t c_begin = tid * a.chunks / T;
+    const uint64_t c_end = (tid + 1) * a.chunks / T;
 
-        uint32_t s[N];
+    uint32_t s[N];
+    if (c_begin < c_end) {
+        const uint64_t start = c_begin << a.log_len;
+        const uint64_t gstart = start ^ (start >> 1);
 #pragma unroll
         for (int i = 0; i < N; i++) s[i] = init[i];
         for (int j = 0; j < NCOL; j++) {
@@ -109,22 +111,34 @@ glynn_m32_kernel(M32Args a) {
                 for (int i = 0; i < N; i++) s[i] = m32_addmod(s[i], col[i], p);
             }
         }
+    }
 
+    for (uint64_t c = c_begin; c < c_end; c++) {
+        if (((c - c_begin) & 255) == 0 && *a.abort_flag) { aborted = true; break; }
+        // bits 0..log_len of the global state index g = c * 2^log_len + i
+        const uint32_t hib = (uint32_t)(c & 1) << a.log_len;
         unsigned long long acc_e = 0, acc_o = 0;
         for (uint32_t q = 0; q < Q; q++) {
             const uint32_t g32 = (q << LOGU) | hib;
 #pragma unroll
             for (int r = 0; r < U; r++) {
-                if (r != 0 || q != 0) {
-                    int j, sub;
-                    if (r != 0) {
-                        j = ctz_small(r);
-                        if (j + 1 < LOGU) sub = ((r >> (j + 1)) & 1) == 0;
-                        else sub = ((g32 >> LOGU) & 1) == 0;
-                    } else {
-                        j = __ffs(q) - 1 + LOGU;
-                        sub = ((g32 >> (j + 1)) & 1) == 0;
-                    }
+                bool step = true;
+                int j, sub;
+                if (r != 0) {
+                    j = ctz_small(r);
+                    if (j + 1 < LOGU) sub = ((r >> (j + 1)) & 1) == 0;
+                    else sub = ((g32 >> LOGU) & 1) == 0;
+                } else if (q != 0) {
+                    j = __ffs(q) - 1 + LOGU;
+                    sub = ((g32 >> (j + 1)) & 1) == 0;
+                } else {
+                    // chunk boundary (lanes may toggle different columns)
+                    step = c != c_begin;
+                    const int jc = __ffsll((long long)c) - 1;
+                    j = a.log_len + jc;
+                    sub = ((c >> (jc + 1)) & 1) == 0;
+                }
+                if (step) {
                     const uint4 *col =
                         reinterpret_cast<const uint4 *>(tab + (2 * j + sub) * NP);
 #pragma unroll
@@ -155,19 +169,18 @@ glynn_m32_kernel(M32Args a) {
                 } else {
                     prod = ch[0];
                 }
+                // Glynn sign (-1)^g = (-1)^r: chunks start at even states
                 if (r & 1) acc_o += prod;
                 else acc_e += prod;
             }
         }
-        // chunk sign: (-1)^popcount(gray(start)); local step i adds (-1)^i
         const uint32_t e = (uint32_t)(acc_e % p), o = (uint32_t)(acc_o % p);
-        uint32_t v;
-        if (__popcll(gstart) & 1) v = o >= e ? o - e : o + (p - e);
-        else v = e >= o ? e - o : e + (p - o);
-        thread_sum += v;
+        thread_sum += e >= o ? e - o : e + (p - o);
     }
 
-    // block reduction of the per-thread sums (each < 2^55 by the host plan)
+    // block reduction of the per-thread residues (< 2^31 each after the
+    // fold, so the 64-bit atomic sum over all blocks cannot overflow)
+    thread_sum %= p;
     __shared__ unsigned long long red[8];
     __shared__ int any_abort;
     if (threadIdx.x == 0) any_abort = 0;

@@ -141,13 +141,24 @@ static int plan_build(const int64_t *A, int n, ExactPlan *P) {
             tab[(2 * j + 1) * NP + ii] = (int32_t)(-2 * row[j]);
         }
     }
+    // One resident wave of blocks (occupancy-limited), each thread owning a
+    // contiguous range of ~128 chunks of >= 64 states; small orders use
+    // fewer blocks so every thread still gets >= 512 states.
     const int occ = occupancy_exact_any(N, G);
-    const uint64_t capacity = (uint64_t)occ * dev.sm_count * 256;
-    P->chunks = plan_chunks(n - 1, 1, 4 * capacity);
-    uint64_t blocks = (P->chunks.chunks + 255) / 256;
-    const uint64_t max_blocks = capacity / 256;
-    if (blocks > max_blocks) blocks = max_blocks;
-    P->blocks = blocks < 1 ? 1 : blocks;
+    const int log_states = n - 1;
+    uint64_t blocks = (uint64_t)occ * dev.sm_count;
+    while (blocks > 1 && ((1ull << log_states) >> 9) < blocks * 256) blocks >>= 1;
+    const uint64_t T = blocks * 256;
+    int log_T = 0;
+    while ((2ull << log_T) <= T) log_T++;
+    int log_len = log_states - (log_T + 7);
+    const int min_len = log_states < 6 ? log_states : 6;
+    if (log_len < min_len) log_len = min_len;
+    if (log_len > 30) log_len = 30;
+    if (log_len < 1) log_len = 1;
+    P->chunks.log_len = log_len;
+    P->chunks.chunks = 1ull << (log_states - log_len);
+    P->blocks = blocks;
     return PG_OK;
 }
 

@@ -201,18 +201,24 @@ static int glynn_m32_batch(const uint64_t *mats, int n, const uint64_t *moduli,
         }
     }
 
-    // Launch shape: aim for ~4 resident waves of 256-thread blocks overall.
+    // Launch shape: one resident wave of blocks shared by the k moduli; each
+    // thread owns a contiguous range of ~128 chunks of >= 64 states (small
+    // orders use fewer blocks so every thread keeps >= 512 states).
     const int occ = occupancy_m32_any(N);
-    const uint64_t capacity_threads = (uint64_t)occ * dev.sm_count * 256;
-    const uint64_t per_mod_target = (4 * capacity_threads + k - 1) / k;
-    const int min_log_len = n - 1 < 1 ? n - 1 : 1;
-    ChunkPlan pl = plan_chunks(n - 1, min_log_len, per_mod_target);
-    uint64_t blocks = (pl.chunks + 255) / 256;
-    const uint64_t max_blocks = (capacity_threads + 255) / 256;
-    uint64_t bpm = blocks;
-    if (bpm * k > max_blocks) bpm = (max_blocks + k - 1) / k;
+    const int log_states = n - 1;
+    uint64_t bpm = ((uint64_t)occ * dev.sm_count + k - 1) / k;
+    while (bpm > 1 && ((1ull << log_states) >> 9) < bpm * 256) bpm >>= 1;
     if (bpm < 1) bpm = 1;
     if (bpm > 65535) bpm = 65535;
+    int log_T = 0;
+    while ((2ull << log_T) <= bpm * 256) log_T++;
+    ChunkPlan pl;
+    pl.log_len = log_states - (log_T + 7);
+    const int min_len = log_states < 6 ? log_states : 6;
+    if (pl.log_len < min_len) pl.log_len = min_len;
+    if (pl.log_len > 30) pl.log_len = 30;
+    if (pl.log_len < 1) pl.log_len = 1;
+    pl.chunks = 1ull << (log_states - pl.log_len);
 
     M32Args args;
     args.tabs = (const uint32_t *)(d + off_tab);
