@@ -25,7 +25,23 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "acc_chain.cuh"
+
+#ifndef EXACT_LOGU
+#define EXACT_LOGU 1
+#endif
+#ifndef EXACT_ACC_PTX
+#define EXACT_ACC_PTX 1
+#endif
+#ifndef EXACT_MIN_BLOCKS
+#define EXACT_MIN_BLOCKS 0
+#endif
+
 namespace pg {
+
+__device__ __forceinline__ constexpr int exact_ctz_small(int r) {
+    return (r & 1) ? 0 : (r & 2) ? 1 : (r & 4) ? 2 : (r & 8) ? 3 : 4;
+}
 
 struct ExactArgs {
     const int32_t *tab;        // [N-1][2][NP]  +2a_ij (dir 0) / -2a_ij (dir 1)
@@ -45,7 +61,8 @@ struct ExactShape {
 };
 
 __host__ __device__ constexpr int exact_min_blocks(int N) {
-    return (65536 / (256 * (N + 48))) < 1 ? 1
+    return EXACT_MIN_BLOCKS > 0 ? EXACT_MIN_BLOCKS
+           : (65536 / (256 * (N + 48))) < 1 ? 1
            : (65536 / (256 * (N + 48))) > 4 ? 4
            : (65536 / (256 * (N + 48)));
 }
@@ -55,6 +72,9 @@ __global__ void __launch_bounds__(256, exact_min_blocks(N))
 exact_glynn_kernel(ExactArgs a) {
     using S = ExactShape<N, G>;
     constexpr int NP = S::NP, NG = S::NG, NL = S::NL, NCOL = N - 1;
+    // steps unrolled per inner iteration (2^LOGU); chunks hold >= 2^LOGU states
+    constexpr int LOGU = (N - 1) < EXACT_LOGU ? (N - 1) : EXACT_LOGU;
+    constexpr int U = 1 << LOGU;
     extern __shared__ int4 esmem[];
     int32_t *tab = reinterpret_cast<int32_t *>(esmem);
     for (int i = threadIdx.x; i < NCOL * 2 * NP / 4; i += blockDim.x)
@@ -65,7 +85,7 @@ exact_glynn_kernel(ExactArgs a) {
 #pragma unroll
     for (int l = 0; l < NL; l++) acc[l] = 0;
     bool aborted = false;
-    const uint32_t Q = (1u << a.log_len) >> 1;
+    const uint32_t Q = (1u << a.log_len) >> LOGU;
 
     // Each thread walks one contiguous, balanced range of chunks
     // [c_begin, c_end): the row sums are initialised once, and crossing a
@@ -94,16 +114,17 @@ exact_glynn_kernel(ExactArgs a) {
         if (((c - c_begin) & 255) == 0 && *a.abort_flag) { aborted = true; break; }
         const uint32_t hib = (uint32_t)(c & 1) << a.log_len;
         for (uint32_t q = 0; q < Q; q++) {
-            const uint32_t g32 = (q << 1) | hib;
+            const uint32_t g32 = (q << LOGU) | hib;
 #pragma unroll
-            for (int r = 0; r < 2; r++) {
+            for (int r = 0; r < U; r++) {
                 bool step = true;
                 int j, sub;
                 if (r != 0) {
-                    j = 0;
-                    sub = ((g32 >> 1) & 1) == 0;
+                    j = exact_ctz_small(r);
+                    if (j + 1 < LOGU) sub = ((r >> (j + 1)) & 1) == 0;
+                    else sub = ((g32 >> LOGU) & 1) == 0;
                 } else if (q != 0) {
-                    j = __ffs(q);  // ctz(q) + 1
+                    j = __ffs(q) - 1 + LOGU;
                     sub = ((g32 >> (j + 1)) & 1) == 0;
                 } else {
                     // chunk boundary g = c * 2^log_len (lanes may differ here)
@@ -127,7 +148,7 @@ exact_glynn_kernel(ExactArgs a) {
                 // exact group products (|x| < 2^31 by the host's grouping);
                 // the term's sign is the XOR of the group signs and the
                 // Glynn sign (-1)^g = (-1)^r (chunks start at even states)
-                uint32_t sx = (uint32_t)r << 31;
+                uint32_t sx = (uint32_t)(r & 1) << 31;
                 uint32_t mag[NG];
 #pragma unroll
                 for (int g = 0; g < NG; g++) {
@@ -138,7 +159,6 @@ exact_glynn_kernel(ExactArgs a) {
                     sx ^= (uint32_t)x;
                     mag[g] = (uint32_t)abs(x);
                 }
-                const uint32_t negx = sx >> 31;
                 // magnitude as an NG-word integer: P = prod mag[g]
                 uint32_t P[NG];
                 P[0] = mag[0];
@@ -153,8 +173,11 @@ exact_glynn_kernel(ExactArgs a) {
                     }
                     P[g] = carry;
                 }
-                // acc += (-1)^negx * P   (conditional two's-complement negate)
-                const uint32_t m = 0u - (negx & 1u);
+                // acc += (-1)^sign * P   (conditional two's-complement negate)
+                const uint32_t m = (uint32_t)((int32_t)sx >> 31);
+#if EXACT_ACC_PTX
+                AccChain<NL, NG>::add(acc, P, m);
+#else
                 uint32_t cy = m & 1u;
 #pragma unroll
                 for (int l = 0; l < NL; l++) {
@@ -163,6 +186,7 @@ exact_glynn_kernel(ExactArgs a) {
                     acc[l] = (uint32_t)t;
                     cy = (uint32_t)(t >> 32);
                 }
+#endif
             }
         }
     }

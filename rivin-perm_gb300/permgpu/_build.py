@@ -44,10 +44,16 @@ def _newest_header() -> float:
 
 
 def build(verbose: bool = False, jobs: int | None = None,
-          extra_flags: list[str] | None = None) -> Path:
-    """Compile every CUDA translation unit and link libpermgpu.so."""
+          extra_flags: list[str] | None = None, lib_path: Path | None = None,
+          build_dir: Path | None = None) -> Path:
+    """Compile every CUDA translation unit and link libpermgpu.so.
+
+    ``extra_flags`` (e.g. tuning macros), ``lib_path`` and ``build_dir``
+    allow building variants of the library side by side."""
     nvcc = _nvcc()
-    BUILD.mkdir(exist_ok=True)
+    LIB = Path(lib_path) if lib_path else globals()["LIB"]
+    BUILD = Path(build_dir) if build_dir else globals()["BUILD"]
+    BUILD.mkdir(parents=True, exist_ok=True)
     sources = sorted(CSRC.glob("*.cu"))
     hdr = _newest_header()
     flags = ARCH + NVCC_FLAGS + list(extra_flags or [])
