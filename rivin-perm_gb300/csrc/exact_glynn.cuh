@@ -28,7 +28,7 @@
 #include "acc_chain.cuh"
 
 #ifndef EXACT_LOGU
-#define EXACT_LOGU 1
+#define EXACT_LOGU 2
 #endif
 #ifndef EXACT_ACC_PTX
 #define EXACT_ACC_PTX 1
