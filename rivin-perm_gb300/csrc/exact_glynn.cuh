@@ -26,12 +26,16 @@
 #include <stdint.h>
 
 #include "acc_chain.cuh"
+#include "mp_mul.cuh"
 
 #ifndef EXACT_LOGU
 #define EXACT_LOGU 2
 #endif
 #ifndef EXACT_ACC_PTX
 #define EXACT_ACC_PTX 1
+#endif
+#ifndef EXACT_MUL_PTX
+#define EXACT_MUL_PTX 1
 #endif
 #ifndef EXACT_MIN_BLOCKS
 #define EXACT_MIN_BLOCKS 0
@@ -42,6 +46,31 @@ namespace pg {
 __device__ __forceinline__ constexpr int exact_ctz_small(int r) {
     return (r & 1) ? 0 : (r & 2) ? 1 : (r & 4) ? 2 : (r & 8) ? 3 : 4;
 }
+
+// P[0..NG-1] = prod_{g < NG} mag[g], one word multiply per group (g words
+// times one word, growing the product by one word each time).
+template <int G0, int NG>
+struct ProdChain {
+    static __device__ __forceinline__ void run(uint32_t *P, const uint32_t *mag) {
+#if EXACT_MUL_PTX
+        MulWord<G0>::apply(P, mag[G0]);
+#else
+        uint32_t carry = 0;
+#pragma unroll
+        for (int l = 0; l < G0; l++) {
+            const uint64_t t = (uint64_t)P[l] * mag[G0] + carry;
+            P[l] = (uint32_t)t;
+            carry = (uint32_t)(t >> 32);
+        }
+        P[G0] = carry;
+#endif
+        ProdChain<G0 + 1, NG>::run(P, mag);
+    }
+};
+template <int NG>
+struct ProdChain<NG, NG> {
+    static __device__ __forceinline__ void run(uint32_t *, const uint32_t *) {}
+};
 
 struct ExactArgs {
     const int32_t *tab;        // [N-1][2][NP]  +2a_ij (dir 0) / -2a_ij (dir 1)
@@ -162,17 +191,7 @@ exact_glynn_kernel(ExactArgs a) {
                 // magnitude as an NG-word integer: P = prod mag[g]
                 uint32_t P[NG];
                 P[0] = mag[0];
-#pragma unroll
-                for (int g = 1; g < NG; g++) {
-                    uint32_t carry = 0;
-#pragma unroll
-                    for (int l = 0; l < g; l++) {
-                        const uint64_t t = (uint64_t)P[l] * mag[g] + carry;
-                        P[l] = (uint32_t)t;
-                        carry = (uint32_t)(t >> 32);
-                    }
-                    P[g] = carry;
-                }
+                ProdChain<1, NG>::run(P, mag);
                 // acc += (-1)^sign * P   (conditional two's-complement negate)
                 const uint32_t m = (uint32_t)((int32_t)sx >> 31);
 #if EXACT_ACC_PTX
