@@ -122,6 +122,36 @@ int pg_exact_plan_info(const pg_exact_plan *plan, int *group, int *words,
 void pg_exact_plan_destroy(pg_exact_plan *plan);
 
 /*
+ * Batched exact engine: per(A_m) for `count` matrices of uneven order in one
+ * persistent, work-stealing launch captured in a CUDA graph.  Matrix m is
+ * the row-major n_m x n_m block at A + offsets[m] (n_m = orders[m]).
+ * out receives `limbs` two's-complement words per matrix.  Orders 2..32
+ * whose rows group into products < 2^31 run inside the batched kernel; any
+ * other matrix is evaluated by pg_exact_permanent when results are
+ * collected (PG_EOVERFLOW if even that engine cannot take it).  Replaces a
+ * per-matrix loop over perm.matrix_permanent(A, method="generic")
+ * (perm.py:1076-1212); there is no batched entry point in the reference.
+ * pg_batch_tune fields <= 0 select the defaults (13, 6, 2).
+ */
+typedef struct {
+    int lane_log_states;   /* log2 Gray states per lane per task */
+    int chunk_log_len;     /* log2 states per aligned chunk */
+    int blocks_per_sm;     /* resident blocks of 256 threads per SM */
+} pg_batch_tune;
+typedef struct pg_batch_plan pg_batch_plan;
+int pg_batch_plan_create(const int64_t *A, const int64_t *offsets,
+                         const int32_t *orders, int count,
+                         const pg_batch_tune *tune, pg_batch_plan **plan);
+int pg_batch_plan_launch(pg_batch_plan *plan, void *stream);
+int pg_batch_plan_result(pg_batch_plan *plan, void *stream, uint32_t *out,
+                         int limbs);
+int pg_batch_plan_info(const pg_batch_plan *plan, uint32_t *tasks,
+                       int *blocks, uint64_t *kernel_states, int *external);
+void pg_batch_plan_destroy(pg_batch_plan *plan);
+int pg_batch_exact(const int64_t *A, const int64_t *offsets,
+                   const int32_t *orders, int count, uint32_t *out, int limbs);
+
+/*
  * Integer-pipe throughput probe (roofline denominator; no reference
  * counterpart): variant 0 mad.lo.u32, 1 mad.wide.u32, 2 mad.hi.u32,
  * 3 add.u32; writes thread-instructions per second for the whole GPU.

@@ -1,0 +1,468 @@
+// Batched exact Glynn engine: thousands of integer matrices of uneven order
+// in one persistent, work-stealing launch captured in a CUDA graph.
+//
+// Work unit ("task"): 32 lanes x k chunks of one matrix; lane l walks chunks
+// [c0 + l*k, c0 + (l+1)*k), so all lanes share the chunk-local Gray columns
+// and the matrix's column table, staged per warp in shared memory.  Warps
+// take tasks from a global atomic counter; the host orders tasks by
+// decreasing work (largest orders first) so the tail is made of small
+// tasks.  Each task's per-word sums are warp-reduced and added to the
+// matrix's 64-bit words with one atomic per word.  Orders 2..32 are compiled
+// (row groups of 4, as in the single-matrix engine); matrices outside that
+// range or whose groups do not fit are evaluated by the single-matrix exact
+// engine when the results are collected.
+//
+// Tuning knobs (pg_batch_tune): log2 states per lane per task, blocks per
+// SM, chunk length.  permgpu.autotune searches them and persists the best.
+#include "pg_internal.h"
+#include "exact_glynn.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+namespace pg {
+
+int exact_run(const int64_t *A, int n, uint32_t *out, int limbs);
+
+static constexpr int BATCH_MAX_N = 32;
+static constexpr int BATCH_NP = 32;                  // row stride in the per-warp slice
+static constexpr int BATCH_SLICE = (BATCH_MAX_N - 1) * 2 * BATCH_NP + BATCH_NP;  // int32 per warp
+static constexpr int BATCH_WORDS = 10;               // accumulator words per matrix
+
+struct BatchTask {
+    uint32_t m;      // matrix index
+    uint32_t k;      // chunks per lane
+    uint64_t c0;     // first chunk of lane 0
+};
+
+struct BatchArgs {
+    const int32_t *tables;        // concatenated [tab | init] per matrix
+    const uint64_t *table_off;    // int32 offset of each matrix's table
+    const uint8_t *orders;        // n per matrix
+    const uint8_t *log_len;       // chunk log length per matrix
+    const uint64_t *chunks;       // chunks per matrix
+    const BatchTask *tasks;
+    uint32_t ntasks;
+    unsigned int *counter;        // zeroed per launch
+    unsigned long long *acc;      // [count][BATCH_WORDS]
+    int *status;
+    volatile const int *abort_flag;
+};
+
+template <int N>
+__device__ __forceinline__ void batch_task(const int32_t *wtab, const BatchArgs &a,
+                                           const BatchTask &t, int lane) {
+    constexpr int G = N >= 4 ? 4 : N;
+    using S = ExactShape<N, G>;
+    constexpr int NP = S::NP, NL = S::NL;
+    // the warp slice stores rows with stride BATCH_NP; exact_walk indexes
+    // with NP, so the host packs each table with stride NP inside the slice
+    const int log_len = a.log_len[t.m];
+    const uint64_t nch = a.chunks[t.m];
+    uint64_t cb = t.c0 + (uint64_t)lane * t.k;
+    uint64_t ce = cb + t.k;
+    if (cb > nch) cb = nch;
+    if (ce > nch) ce = nch;
+    uint32_t acc[NL];
+#pragma unroll
+    for (int l = 0; l < NL; l++) acc[l] = 0;
+    bool ok = true;
+    if (cb < ce) {
+        int32_t s[N];
+        exact_init<N>(wtab, wtab + (N - 1) * 2 * NP, s, cb << log_len);
+        ok = exact_walk<N, G>(wtab, s, acc, cb, ce, log_len, a.abort_flag);
+    }
+    if (!ok) atomicExch(a.status, 1);
+#pragma unroll
+    for (int l = 0; l < NL; l++) {
+        long long v = (l == NL - 1) ? (long long)(int32_t)acc[l] : (long long)acc[l];
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+        if (lane == 0 && v != 0)
+            atomicAdd(a.acc + (size_t)t.m * BATCH_WORDS + l, (unsigned long long)v);
+    }
+}
+
+__global__ void __launch_bounds__(256, 2) batch_glynn_kernel(BatchArgs a) {
+    extern __shared__ int4 bsmem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int32_t *wtab = reinterpret_cast<int32_t *>(bsmem) + warp * BATCH_SLICE;
+    uint32_t cur = 0xffffffffu;
+    for (;;) {
+        unsigned int ti = 0;
+        if (lane == 0) ti = atomicAdd(a.counter, 1u);
+        ti = __shfl_sync(0xffffffffu, ti, 0);
+        if (ti >= a.ntasks) break;
+        const BatchTask t = a.tasks[ti];
+        const int n = a.orders[t.m];
+        if (t.m != cur) {
+            const int NP = (n + 3) & ~3;
+            const int words = (n - 1) * 2 * NP + NP;
+            const int32_t *src = a.tables + a.table_off[t.m];
+            __syncwarp();
+            for (int i = lane; i < words; i += 32) wtab[i] = __ldg(src + i);
+            __syncwarp();
+            cur = t.m;
+        }
+        switch (n) {
+#define PG_BATCH_CASE(NN) case NN: batch_task<NN>(wtab, a, t, lane); break;
+            PG_BATCH_CASE(2) PG_BATCH_CASE(3) PG_BATCH_CASE(4) PG_BATCH_CASE(5)
+            PG_BATCH_CASE(6) PG_BATCH_CASE(7) PG_BATCH_CASE(8) PG_BATCH_CASE(9)
+            PG_BATCH_CASE(10) PG_BATCH_CASE(11) PG_BATCH_CASE(12) PG_BATCH_CASE(13)
+            PG_BATCH_CASE(14) PG_BATCH_CASE(15) PG_BATCH_CASE(16) PG_BATCH_CASE(17)
+            PG_BATCH_CASE(18) PG_BATCH_CASE(19) PG_BATCH_CASE(20) PG_BATCH_CASE(21)
+            PG_BATCH_CASE(22) PG_BATCH_CASE(23) PG_BATCH_CASE(24) PG_BATCH_CASE(25)
+            PG_BATCH_CASE(26) PG_BATCH_CASE(27) PG_BATCH_CASE(28) PG_BATCH_CASE(29)
+            PG_BATCH_CASE(30) PG_BATCH_CASE(31) PG_BATCH_CASE(32)
+#undef PG_BATCH_CASE
+        default: break;
+        }
+    }
+}
+
+static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// words += v * 2^(32*pos) in W-word two's complement
+static void add_i64_at(std::vector<uint32_t> &w, int pos, long long v) {
+    const int W = (int)w.size();
+    const uint32_t ext = v < 0 ? 0xffffffffu : 0u;
+    uint64_t carry = 0;
+    for (int i = pos; i < W; i++) {
+        uint32_t add = i == pos ? (uint32_t)(uint64_t)v
+                     : i == pos + 1 ? (uint32_t)((uint64_t)v >> 32) : ext;
+        const uint64_t t = (uint64_t)w[i] + add + carry;
+        w[i] = (uint32_t)t;
+        carry = t >> 32;
+    }
+}
+
+// Row order for groups of 4 (every group's bound product < 2^31), or false.
+static bool batch_group(const int64_t *A, int n, std::vector<int> *order) {
+    const int G = n >= 4 ? 4 : n;
+    const int NG = (n + G - 1) / G;
+    std::vector<uint64_t> B(n);
+    for (int i = 0; i < n; i++) {
+        unsigned __int128 s = 0;
+        for (int j = 0; j < n; j++) {
+            const int64_t v = A[(size_t)i * n + j];
+            s += v < 0 ? (unsigned __int128)(-(__int128)v) : (unsigned __int128)v;
+        }
+        if (s >= ((unsigned __int128)1 << 30)) return false;
+        B[i] = (uint64_t)s;
+    }
+    std::vector<int> rows(n);
+    for (int i = 0; i < n; i++) rows[i] = i;
+    std::stable_sort(rows.begin(), rows.end(), [&](int x, int y) { return B[x] > B[y]; });
+    std::vector<int> cap(NG, G);
+    cap[NG - 1] = n - (NG - 1) * G;
+    std::vector<double> lp(NG, 0.0);
+    std::vector<std::vector<int>> mem(NG);
+    for (int r : rows) {
+        int best = -1;
+        for (int g = 0; g < NG; g++) {
+            if ((int)mem[g].size() >= cap[g]) continue;
+            if (best < 0 || lp[g] < lp[best]) best = g;
+        }
+        mem[best].push_back(r);
+        lp[best] += std::log2((double)(B[r] ? B[r] : 1));
+    }
+    for (auto &g : mem) {
+        unsigned __int128 p = 1;
+        for (int r : g) {
+            p *= (B[r] ? B[r] : 1);
+            if (p >= ((unsigned __int128)1 << 31)) return false;
+        }
+    }
+    order->clear();
+    for (auto &g : mem)
+        for (int r : g) order->push_back(r);
+    return true;
+}
+
+struct BatchPlan {
+    int count = 0;
+    std::vector<int> orders;
+    std::vector<uint8_t> in_kernel;        // 1 if the batch kernel evaluates it
+    std::vector<std::vector<int64_t>> external;  // matrices for the single engine
+    std::vector<int> ext_index;
+    std::vector<double> bound_bits;
+    size_t total = 0, off_acc = 0, off_counter = 0, off_status = 0;
+    uint32_t ntasks = 0;
+    int blocks = 0;
+    size_t smem = 0;
+    char *dev = nullptr;
+    char *host = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    BatchArgs args{};
+    uint64_t kernel_states = 0;
+};
+
+}  // namespace pg
+
+struct pg_batch_plan {
+    pg::BatchPlan p;
+};
+
+extern "C" {
+
+int pg_batch_plan_create(const int64_t *A, const int64_t *offsets, const int32_t *orders,
+                         int count, const pg_batch_tune *tune, pg_batch_plan **out) {
+    using namespace pg;
+    if (!out) return fail(PG_EINVAL, "out is null");
+    *out = nullptr;
+    if (count < 0 || (count > 0 && (!A || !offsets || !orders)))
+        return fail(PG_EINVAL, "batch arguments invalid");
+    DeviceInfo dev;
+    int st = device_info(&dev);
+    if (st != PG_OK) return st;
+    volatile int *abort_dev;
+    st = abort_flag_device(&abort_dev);
+    if (st != PG_OK) return st;
+
+    const int lane_log = tune && tune->lane_log_states > 0 ? tune->lane_log_states : 13;
+    const int chunk_log = tune && tune->chunk_log_len > 0 ? tune->chunk_log_len : 6;
+    const int bps = tune && tune->blocks_per_sm > 0 ? tune->blocks_per_sm : 2;
+
+    pg_batch_plan *h = new pg_batch_plan();
+    BatchPlan &P = h->p;
+    P.count = count;
+    P.orders.assign(orders, orders + count);
+    P.in_kernel.assign(count, 0);
+    P.ext_index.assign(count, -1);
+    P.bound_bits.assign(count, 0.0);
+
+    std::vector<int32_t> tables;
+    std::vector<uint64_t> toff(count, 0), nchunks(count, 0);
+    std::vector<uint8_t> ord8(count, 0), loglen(count, 0);
+    std::vector<BatchTask> tasks;
+    std::vector<uint64_t> task_work;
+    for (int m = 0; m < count; m++) {
+        const int n = orders[m];
+        if (n < 0 || n >= 64) { delete h; return fail(PG_ERANGE, "matrix order must be 0 <= n < 64"); }
+        const int64_t *a = A + offsets[m];
+        double bits = 0;
+        for (int i = 0; i < n; i++) {
+            double rs = 0;
+            for (int j = 0; j < n; j++) rs += std::fabs((double)a[(size_t)i * n + j]);
+            bits += std::log2(rs < 1 ? 1 : rs);
+        }
+        P.bound_bits[m] = bits;
+        std::vector<int> order;
+        if (n < 2 || n > BATCH_MAX_N || !batch_group(a, n, &order)) {
+            P.ext_index[m] = (int)P.external.size();
+            P.external.emplace_back(a, a + (size_t)n * n);
+            continue;
+        }
+        P.in_kernel[m] = 1;
+        const int NP = (n + 3) & ~3;
+        toff[m] = tables.size();
+        const size_t base = tables.size();
+        tables.resize(base + (size_t)(n - 1) * 2 * NP + NP, 0);
+        for (int ii = 0; ii < n; ii++) {
+            const int64_t *row = a + (size_t)order[ii] * n;
+            int64_t sum = 0;
+            for (int j = 0; j < n; j++) sum += row[j];
+            tables[base + (size_t)(n - 1) * 2 * NP + ii] = (int32_t)sum;
+            for (int j = 0; j < n - 1; j++) {
+                tables[base + (size_t)(2 * j + 0) * NP + ii] = (int32_t)(2 * row[j]);
+                tables[base + (size_t)(2 * j + 1) * NP + ii] = (int32_t)(-2 * row[j]);
+            }
+        }
+        const int log_states = n - 1;
+        const int LOGU = log_states < EXACT_LOGU ? log_states : EXACT_LOGU;
+        int ll = chunk_log < log_states ? chunk_log : log_states;
+        if (ll < LOGU) ll = LOGU;
+        if (ll < 1) ll = 1;
+        const uint64_t ch = 1ull << (log_states - ll);
+        uint64_t k = lane_log > ll ? (1ull << (lane_log - ll)) : 1;
+        if (k * 32 > ch) k = (ch + 31) / 32;
+        if (k < 1) k = 1;
+        ord8[m] = (uint8_t)n;
+        loglen[m] = (uint8_t)ll;
+        nchunks[m] = ch;
+        P.kernel_states += 1ull << log_states;
+        for (uint64_t c0 = 0; c0 < ch; c0 += 32 * k) {
+            tasks.push_back(BatchTask{(uint32_t)m, (uint32_t)k, c0});
+            const uint64_t span = std::min<uint64_t>(32 * k, ch - c0);
+            // cost model: states of the busiest lane times per-state work ~ n
+            task_work.push_back(std::min<uint64_t>(k, span) * (1ull << ll) * (uint64_t)n);
+        }
+    }
+    // largest tasks first (LPT order); ties keep matrix order
+    std::vector<uint32_t> idx(tasks.size());
+    for (size_t i = 0; i < idx.size(); i++) idx[i] = (uint32_t)i;
+    std::stable_sort(idx.begin(), idx.end(),
+                     [&](uint32_t x, uint32_t y) { return task_work[x] > task_work[y]; });
+    std::vector<BatchTask> sorted(tasks.size());
+    for (size_t i = 0; i < idx.size(); i++) sorted[i] = tasks[idx[i]];
+    P.ntasks = (uint32_t)sorted.size();
+
+    const size_t off_tables = 0;
+    const size_t off_toff = align_up(off_tables + tables.size() * 4, 256);
+    const size_t off_ord = align_up(off_toff + (size_t)count * 8, 256);
+    const size_t off_ll = align_up(off_ord + (size_t)count, 256);
+    const size_t off_nch = align_up(off_ll + (size_t)count, 256);
+    const size_t off_tasks = align_up(off_nch + (size_t)count * 8, 256);
+    P.off_acc = align_up(off_tasks + sorted.size() * sizeof(BatchTask), 256);
+    P.off_counter = align_up(P.off_acc + (size_t)count * BATCH_WORDS * 8, 256);
+    P.off_status = P.off_counter + 64;
+    P.total = align_up(P.off_status + 64, 256);
+
+    cudaError_t e = cudaMalloc((void **)&P.dev, P.total);
+    if (e == cudaSuccess) e = cudaHostAlloc((void **)&P.host, P.total, cudaHostAllocDefault);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&P.stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        st = cuda_fail(e, "pg_batch_plan_create");
+        pg_batch_plan_destroy(h);
+        return st;
+    }
+    std::memset(P.host, 0, P.total);
+    if (!tables.empty()) std::memcpy(P.host + off_tables, tables.data(), tables.size() * 4);
+    std::memcpy(P.host + off_toff, toff.data(), (size_t)count * 8);
+    std::memcpy(P.host + off_ord, ord8.data(), (size_t)count);
+    std::memcpy(P.host + off_ll, loglen.data(), (size_t)count);
+    std::memcpy(P.host + off_nch, nchunks.data(), (size_t)count * 8);
+    if (!sorted.empty())
+        std::memcpy(P.host + off_tasks, sorted.data(), sorted.size() * sizeof(BatchTask));
+    e = cudaMemcpyAsync(P.dev, P.host, P.off_acc, cudaMemcpyHostToDevice, P.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(P.stream);
+    if (e != cudaSuccess) {
+        st = cuda_fail(e, "pg_batch_plan_create upload");
+        pg_batch_plan_destroy(h);
+        return st;
+    }
+
+    BatchArgs &a = P.args;
+    a.tables = (const int32_t *)(P.dev + off_tables);
+    a.table_off = (const uint64_t *)(P.dev + off_toff);
+    a.orders = (const uint8_t *)(P.dev + off_ord);
+    a.log_len = (const uint8_t *)(P.dev + off_ll);
+    a.chunks = (const uint64_t *)(P.dev + off_nch);
+    a.tasks = (const BatchTask *)(P.dev + off_tasks);
+    a.ntasks = P.ntasks;
+    a.counter = (unsigned int *)(P.dev + P.off_counter);
+    a.acc = (unsigned long long *)(P.dev + P.off_acc);
+    a.status = (int *)(P.dev + P.off_status);
+    a.abort_flag = abort_dev;
+
+    P.smem = (size_t)8 * BATCH_SLICE * sizeof(int32_t);
+    e = cudaFuncSetAttribute(batch_glynn_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)P.smem);
+    int occ = 0;
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_glynn_kernel, 256, P.smem);
+    if (e != cudaSuccess) {
+        st = cuda_fail(e, "batch kernel attributes");
+        pg_batch_plan_destroy(h);
+        return st;
+    }
+    P.blocks = dev.sm_count * std::max(1, std::min(occ, bps));
+
+    // Capture [zero accumulators/counter/status, persistent kernel] once.
+    e = cudaStreamBeginCapture(P.stream, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        cudaMemsetAsync(P.dev + P.off_acc, 0, P.total - P.off_acc, P.stream);
+        if (P.ntasks)
+            batch_glynn_kernel<<<P.blocks, 256, P.smem, P.stream>>>(a);
+        e = cudaStreamEndCapture(P.stream, &P.graph);
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&P.exec, P.graph, 0);
+    if (e != cudaSuccess) {
+        st = cuda_fail(e, "batch graph capture");
+        pg_batch_plan_destroy(h);
+        return st;
+    }
+    *out = h;
+    return PG_OK;
+}
+
+int pg_batch_plan_launch(pg_batch_plan *plan, void *stream) {
+    using namespace pg;
+    if (!plan) return fail(PG_EINVAL, "plan is null");
+    PG_CUDA(cudaGraphLaunch(plan->p.exec, stream ? (cudaStream_t)stream : plan->p.stream));
+    return PG_OK;
+}
+
+int pg_batch_plan_result(pg_batch_plan *plan, void *stream, uint32_t *out, int limbs) {
+    using namespace pg;
+    if (!plan || !out || limbs < 1) return fail(PG_EINVAL, "null argument");
+    BatchPlan &P = plan->p;
+    cudaStream_t s = stream ? (cudaStream_t)stream : P.stream;
+    for (int m = 0; m < P.count; m++)
+        if (P.bound_bits[m] + 2 > 32.0 * limbs)
+            return fail(PG_ERANGE, "limbs per matrix too small for a matrix's bound");
+    PG_CUDA(cudaMemcpyAsync(P.host + P.off_acc, P.dev + P.off_acc, P.total - P.off_acc,
+                            cudaMemcpyDeviceToHost, s));
+    PG_CUDA(cudaStreamSynchronize(s));
+    if (*(int *)(P.host + P.off_status))
+        return fail(PG_EABORT, "batch launch aborted by pg_abort()");
+    const long long *acc = (const long long *)(P.host + P.off_acc);
+    for (int m = 0; m < P.count; m++) {
+        uint32_t *o = out + (size_t)m * limbs;
+        const int n = P.orders[m];
+        if (!P.in_kernel[m]) {
+            const std::vector<int64_t> &a = P.external[P.ext_index[m]];
+            int st = pg_exact_permanent(a.data(), n, o, limbs);
+            if (st != PG_OK) return st;
+            continue;
+        }
+        const int W = BATCH_WORDS + 3;
+        std::vector<uint32_t> S(W, 0);
+        const int G = n >= 4 ? 4 : n;
+        const int NL = (n + G - 1) / G + 1;
+        for (int l = 0; l < NL; l++) add_i64_at(S, l, acc[(size_t)m * BATCH_WORDS + l]);
+        const int sh = n - 1;
+        for (int b = 0; b < sh; b++)
+            if ((S[b >> 5] >> (b & 31)) & 1)
+                return fail(PG_EINTERNAL, "Glynn sum not divisible by 2^(n-1)");
+        const uint32_t ext = (S[W - 1] >> 31) ? 0xffffffffu : 0u;
+        for (int i = 0; i < limbs; i++) {
+            const int bit = 32 * i + sh;
+            const int wi = bit >> 5, bo = bit & 31;
+            const uint32_t lo = wi < W ? S[wi] : ext;
+            const uint32_t hi = wi + 1 < W ? S[wi + 1] : ext;
+            o[i] = bo ? (lo >> bo) | (hi << (32 - bo)) : lo;
+        }
+    }
+    return PG_OK;
+}
+
+int pg_batch_plan_info(const pg_batch_plan *plan, uint32_t *tasks, int *blocks,
+                       uint64_t *kernel_states, int *external) {
+    using namespace pg;
+    if (!plan) return fail(PG_EINVAL, "plan is null");
+    if (tasks) *tasks = plan->p.ntasks;
+    if (blocks) *blocks = plan->p.blocks;
+    if (kernel_states) *kernel_states = plan->p.kernel_states;
+    if (external) *external = (int)plan->p.external.size();
+    return PG_OK;
+}
+
+void pg_batch_plan_destroy(pg_batch_plan *plan) {
+    if (!plan) return;
+    pg::BatchPlan &P = plan->p;
+    if (P.stream) cudaStreamSynchronize(P.stream);
+    if (P.exec) cudaGraphExecDestroy(P.exec);
+    if (P.graph) cudaGraphDestroy(P.graph);
+    if (P.dev) cudaFree(P.dev);
+    if (P.host) cudaFreeHost(P.host);
+    if (P.stream) cudaStreamDestroy(P.stream);
+    delete plan;
+}
+
+int pg_batch_exact(const int64_t *A, const int64_t *offsets, const int32_t *orders,
+                   int count, uint32_t *out, int limbs) {
+    pg_batch_plan *plan = nullptr;
+    int st = pg_batch_plan_create(A, offsets, orders, count, nullptr, &plan);
+    if (st != PG_OK) return st;
+    st = pg_batch_plan_launch(plan, nullptr);
+    if (st == PG_OK) st = pg_batch_plan_result(plan, nullptr, out, limbs);
+    pg_batch_plan_destroy(plan);
+    return st;
+}
+
+}  // extern "C"

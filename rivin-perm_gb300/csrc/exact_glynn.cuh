@@ -6,20 +6,21 @@
 // integer of at most sum_i log2(B_i) bits.  This kernel keeps the row sums
 // exact, multiplies them in groups of G rows with plain 32-bit IMUL (the host
 // permutes rows so that every group's bound product is < 2^31), forms the
-// exact magnitude of the term as an NG-word integer with a mad.wide chain,
-// and adds it with its sign into an NL-word two's-complement accumulator.
+// exact magnitude of the term as an NG-word integer (mul.wide products plus
+// an ALU carry chain), and adds it with its sign into an NL-word
+// two's-complement accumulator.
 //
 // Versus a CRT residue walk this removes the modular reductions and the
 // per-prime repetition: for n = 32, entries in [-8,8], one exact term costs
-// 24 IMUL + 28 IMAD.WIDE, while 8 CRT primes cost 8 * 31 Montgomery
+// 24 IMUL + 28 mul.wide, while 8 CRT primes cost 8 * 31 Montgomery
 // products (~750 IMAD-class instructions) plus 8 * 32 modular row updates.
 //
-// Traversal, sign and chunking are those of the residue kernel (rivin-perm
-// perm_c_omp.c:556-639): states in Gray order, the last column's sign fixed,
-// aligned chunks so a warp shares the toggled column, Glynn sign (-1)^g.
-// Each block adds its per-word sums into 64-bit words acc[w]; the host
-// carries them into one integer S and returns S / 2^(n-1) (checking that
-// the division is exact).
+// Traversal, sign and chunking follow the residue walk of rivin-perm
+// perm_c_omp.c:556-639: states in Gray order with the last column's sign
+// fixed, Glynn sign (-1)^g.  Chunks of 2^log_len states are aligned, so at
+// local step i every lane of a warp toggles column ctz(i) and reads the same
+// table row (shared-memory broadcast).  A thread walks a contiguous range of
+// chunks; crossing a chunk boundary is an ordinary Gray step.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -72,76 +73,79 @@ struct ProdChain<NG, NG> {
     static __device__ __forceinline__ void run(uint32_t *, const uint32_t *) {}
 };
 
-struct ExactArgs {
-    const int32_t *tab;        // [N-1][2][NP]  +2a_ij (dir 0) / -2a_ij (dir 1)
-    const int32_t *init;       // [NP] row sums of the all-plus state
-    unsigned long long *acc;   // [NL] per-word sums (two's complement, zeroed)
-    int *status;
-    volatile const int *abort_flag;
-    uint64_t chunks;
-    int log_len;               // >= 1, <= 30
-};
-
 template <int N, int G>
 struct ExactShape {
     static constexpr int NP = (N + 3) & ~3;
     static constexpr int NG = (N + G - 1) / G;           // product words
     static constexpr int NL = NG + (N > 32 ? 2 : 1);     // accumulator words
+    static constexpr int LOGU = (N - 1) < EXACT_LOGU ? (N - 1) : EXACT_LOGU;
 };
 
-__host__ __device__ constexpr int exact_min_blocks(int N) {
-    return EXACT_MIN_BLOCKS > 0 ? EXACT_MIN_BLOCKS
-           : (65536 / (256 * (N + 48))) < 1 ? 1
-           : (65536 / (256 * (N + 48))) > 4 ? 4
-           : (65536 / (256 * (N + 48)));
-}
-
-template <int N, int G>
-__global__ void __launch_bounds__(256, exact_min_blocks(N))
-exact_glynn_kernel(ExactArgs a) {
-    using S = ExactShape<N, G>;
-    constexpr int NP = S::NP, NG = S::NG, NL = S::NL, NCOL = N - 1;
-    // steps unrolled per inner iteration (2^LOGU); chunks hold >= 2^LOGU states
-    constexpr int LOGU = (N - 1) < EXACT_LOGU ? (N - 1) : EXACT_LOGU;
-    constexpr int U = 1 << LOGU;
-    extern __shared__ int4 esmem[];
-    int32_t *tab = reinterpret_cast<int32_t *>(esmem);
-    for (int i = threadIdx.x; i < NCOL * 2 * NP / 4; i += blockDim.x)
-        esmem[i] = reinterpret_cast<const int4 *>(a.tab)[i];
-    __syncthreads();
-
-    uint32_t acc[NL];
+// Row sums of Gray state `start`: init - sum_{j in gray(start)} 2 a_j.
+template <int N>
+__device__ __forceinline__ void exact_init(const int32_t *tab, const int32_t *init,
+                                           int32_t *s, uint64_t start) {
+    constexpr int NP = (N + 3) & ~3;
+    const uint64_t gs = start ^ (start >> 1);
 #pragma unroll
-    for (int l = 0; l < NL; l++) acc[l] = 0;
-    bool aborted = false;
-    const uint32_t Q = (1u << a.log_len) >> LOGU;
-
-    // Each thread walks one contiguous, balanced range of chunks
-    // [c_begin, c_end): the row sums are initialised once, and crossing a
-    // chunk boundary is an ordinary Gray step (column log_len + ctz(c)).
-    const uint64_t T = (uint64_t)gridDim.x * blockDim.x;
-    const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const uint64_t c_begin = tid * a.chunks / T;
-    const uint64_t c_end = (tid + 1) * a.chunks / T;
-
-    int32_t s[N];
-    if (c_begin < c_end) {
-        const uint64_t start = c_begin << a.log_len;
-        const uint64_t gstart = start ^ (start >> 1);
+    for (int i = 0; i < N; i++) s[i] = init[i];
+    for (int j = 0; j < N - 1; j++) {
+        if ((gs >> j) & 1) {
+            const int32_t *col = tab + (2 * j + 1) * NP;
 #pragma unroll
-        for (int i = 0; i < N; i++) s[i] = a.init[i];
-        for (int j = 0; j < NCOL; j++) {
-            if ((gstart >> j) & 1) {
-                const int32_t *col = tab + (2 * j + 1) * NP;
-#pragma unroll
-                for (int i = 0; i < N; i++) s[i] += col[i];
-            }
+            for (int i = 0; i < N; i++) s[i] += col[i];
         }
     }
+}
 
+// One Glynn term at the current row sums: acc += (-1)^(odd + signs) * prod s.
+template <int N, int G>
+__device__ __forceinline__ void exact_term(const int32_t *s, uint32_t *acc, uint32_t odd) {
+    using S = ExactShape<N, G>;
+    constexpr int NG = S::NG, NL = S::NL;
+    // exact group products (|x| < 2^31 by the host's grouping); the sign is
+    // the XOR of the group signs and the Glynn sign
+    uint32_t sx = odd << 31;
+    uint32_t mag[NG];
+#pragma unroll
+    for (int g = 0; g < NG; g++) {
+        int32_t x = s[g * G];
+#pragma unroll
+        for (int t = 1; t < G; t++)
+            if (g * G + t < N) x *= s[g * G + t];
+        sx ^= (uint32_t)x;
+        mag[g] = (uint32_t)abs(x);
+    }
+    uint32_t P[NG];
+    P[0] = mag[0];
+    ProdChain<1, NG>::run(P, mag);
+    const uint32_t m = (uint32_t)((int32_t)sx >> 31);
+#if EXACT_ACC_PTX
+    AccChain<NL, NG>::add(acc, P, m);
+#else
+    uint32_t cy = m & 1u;
+#pragma unroll
+    for (int l = 0; l < NL; l++) {
+        const uint32_t w = (l < NG ? P[l] : 0u) ^ m;
+        const uint64_t t = (uint64_t)acc[l] + w + cy;
+        acc[l] = (uint32_t)t;
+        cy = (uint32_t)(t >> 32);
+    }
+#endif
+}
+
+// Walk chunks [c_begin, c_end) (row sums s already at state c_begin*2^log_len)
+// adding every term into acc.  Returns false if the abort word was seen.
+template <int N, int G>
+__device__ __forceinline__ bool exact_walk(const int32_t *tab, int32_t *s, uint32_t *acc,
+                                           uint64_t c_begin, uint64_t c_end, int log_len,
+                                           volatile const int *abort_flag) {
+    using S = ExactShape<N, G>;
+    constexpr int NP = S::NP, LOGU = S::LOGU, U = 1 << LOGU;
+    const uint32_t Q = (1u << log_len) >> LOGU;
     for (uint64_t c = c_begin; c < c_end; c++) {
-        if (((c - c_begin) & 255) == 0 && *a.abort_flag) { aborted = true; break; }
-        const uint32_t hib = (uint32_t)(c & 1) << a.log_len;
+        if (((c - c_begin) & 255) == 0 && *abort_flag) return false;
+        const uint32_t hib = (uint32_t)(c & 1) << log_len;
         for (uint32_t q = 0; q < Q; q++) {
             const uint32_t g32 = (q << LOGU) | hib;
 #pragma unroll
@@ -159,7 +163,7 @@ exact_glynn_kernel(ExactArgs a) {
                     // chunk boundary g = c * 2^log_len (lanes may differ here)
                     step = c != c_begin;
                     const int jc = __ffsll((long long)c) - 1;
-                    j = a.log_len + jc;
+                    j = log_len + jc;
                     sub = ((c >> (jc + 1)) & 1) == 0;
                 }
                 if (step) {
@@ -174,40 +178,59 @@ exact_glynn_kernel(ExactArgs a) {
                         if (4 * v + 3 < N) s[4 * v + 3] += d.w;
                     }
                 }
-                // exact group products (|x| < 2^31 by the host's grouping);
-                // the term's sign is the XOR of the group signs and the
-                // Glynn sign (-1)^g = (-1)^r (chunks start at even states)
-                uint32_t sx = (uint32_t)(r & 1) << 31;
-                uint32_t mag[NG];
-#pragma unroll
-                for (int g = 0; g < NG; g++) {
-                    int32_t x = s[g * G];
-#pragma unroll
-                    for (int t = 1; t < G; t++)
-                        if (g * G + t < N) x *= s[g * G + t];
-                    sx ^= (uint32_t)x;
-                    mag[g] = (uint32_t)abs(x);
-                }
-                // magnitude as an NG-word integer: P = prod mag[g]
-                uint32_t P[NG];
-                P[0] = mag[0];
-                ProdChain<1, NG>::run(P, mag);
-                // acc += (-1)^sign * P   (conditional two's-complement negate)
-                const uint32_t m = (uint32_t)((int32_t)sx >> 31);
-#if EXACT_ACC_PTX
-                AccChain<NL, NG>::add(acc, P, m);
-#else
-                uint32_t cy = m & 1u;
-#pragma unroll
-                for (int l = 0; l < NL; l++) {
-                    const uint32_t w = (l < NG ? P[l] : 0u) ^ m;
-                    const uint64_t t = (uint64_t)acc[l] + w + cy;
-                    acc[l] = (uint32_t)t;
-                    cy = (uint32_t)(t >> 32);
-                }
-#endif
+                // chunks start at even states, so (-1)^g = (-1)^r
+                exact_term<N, G>(s, acc, (uint32_t)(r & 1));
             }
         }
+    }
+    return true;
+}
+
+struct ExactArgs {
+    const int32_t *tab;        // [N-1][2][NP]  +2a_ij (dir 0) / -2a_ij (dir 1)
+    const int32_t *init;       // [NP] row sums of the all-plus state
+    unsigned long long *acc;   // [NL] per-word sums (two's complement, zeroed)
+    int *status;
+    volatile const int *abort_flag;
+    uint64_t chunks;
+    int log_len;               // >= LOGU, <= 30
+};
+
+// Resident blocks per SM requested from ptxas: a register budget of about
+// N + 64 per thread (row sums plus the product/accumulator words) measured
+// fastest; tighter budgets spill.
+__host__ __device__ constexpr int exact_min_blocks(int N) {
+    return EXACT_MIN_BLOCKS > 0 ? EXACT_MIN_BLOCKS
+           : (65536 / (256 * (N + 64))) < 1 ? 1
+           : (65536 / (256 * (N + 64))) > 4 ? 4
+           : (65536 / (256 * (N + 64)));
+}
+
+template <int N, int G>
+__global__ void __launch_bounds__(256, exact_min_blocks(N))
+exact_glynn_kernel(ExactArgs a) {
+    using S = ExactShape<N, G>;
+    constexpr int NP = S::NP, NL = S::NL, NCOL = N - 1;
+    extern __shared__ int4 esmem[];
+    int32_t *tab = reinterpret_cast<int32_t *>(esmem);
+    for (int i = threadIdx.x; i < NCOL * 2 * NP / 4; i += blockDim.x)
+        esmem[i] = reinterpret_cast<const int4 *>(a.tab)[i];
+    __syncthreads();
+
+    uint32_t acc[NL];
+#pragma unroll
+    for (int l = 0; l < NL; l++) acc[l] = 0;
+
+    // one contiguous, balanced range of chunks per thread
+    const uint64_t T = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t c_begin = tid * a.chunks / T;
+    const uint64_t c_end = (tid + 1) * a.chunks / T;
+    bool aborted = false;
+    if (c_begin < c_end) {
+        int32_t s[N];
+        exact_init<N>(tab, a.init, s, c_begin << a.log_len);
+        aborted = !exact_walk<N, G>(tab, s, acc, c_begin, c_end, a.log_len, a.abort_flag);
     }
 
     // Block reduction: word l < NL-1 contributes acc[l] (unsigned), the top

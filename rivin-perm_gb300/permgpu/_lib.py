@@ -59,7 +59,21 @@ SIGNATURES = {
     "pg_exact_plan_info": ([ctypes.c_void_p, _c_intp, _c_intp, _c_u64p, _c_u64p, _c_u64p], ctypes.c_int),
     "pg_exact_plan_destroy": ([ctypes.c_void_p], None),
     "pg_probe_int_throughput": ([ctypes.c_int, ctypes.c_int, _c_f64p], ctypes.c_int),
+    "pg_batch_plan_create": ([_c_i64p, _c_i64p, _c_i32p, ctypes.c_int, ctypes.c_void_p,
+                              ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
+    "pg_batch_plan_launch": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "pg_batch_plan_result": ([ctypes.c_void_p, ctypes.c_void_p, _c_u32p, ctypes.c_int], ctypes.c_int),
+    "pg_batch_plan_info": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint32), _c_intp, _c_u64p,
+                            _c_intp], ctypes.c_int),
+    "pg_batch_plan_destroy": ([ctypes.c_void_p], None),
+    "pg_batch_exact": ([_c_i64p, _c_i64p, _c_i32p, ctypes.c_int, _c_u32p, ctypes.c_int], ctypes.c_int),
 }
+
+
+class BatchTune(ctypes.Structure):
+    """pg_batch_tune: fields <= 0 select the library defaults."""
+    _fields_ = [("lane_log_states", ctypes.c_int), ("chunk_log_len", ctypes.c_int),
+                ("blocks_per_sm", ctypes.c_int)]
 
 _lib = None
 _lock = threading.Lock()
@@ -211,6 +225,79 @@ class ExactPlan:
             self.close()
         except Exception:
             pass
+
+
+def pack_batch(matrices):
+    """(A_packed int64, offsets int64, orders int32) for a list of square
+    integer matrices."""
+    orders = np.array([np.asarray(m).shape[0] if np.asarray(m).ndim == 2 else 0
+                       for m in matrices], dtype=np.int32)
+    sizes = orders.astype(np.int64) ** 2
+    offsets = np.zeros(len(matrices), dtype=np.int64)
+    if len(matrices) > 1:
+        offsets[1:] = np.cumsum(sizes)[:-1]
+    packed = np.zeros(int(sizes.sum()) or 1, dtype=np.int64)
+    for m, off, sz in zip(matrices, offsets, sizes):
+        if sz:
+            packed[off:off + sz] = np.asarray(m, dtype=np.int64).reshape(-1)
+    return packed, offsets, orders
+
+
+def batch_limbs(matrices) -> int:
+    return max([exact_limbs(np.asarray(m)) for m in matrices if np.asarray(m).size] or [2])
+
+
+class BatchPlan:
+    """Device-resident batched exact evaluation (pg_batch_plan_*): one
+    persistent work-stealing launch per evaluation, replayed from a CUDA
+    graph."""
+
+    def __init__(self, matrices, tune: tuple | None = None):
+        self.count = len(matrices)
+        self.limbs = batch_limbs(matrices)
+        packed, offsets, orders = pack_batch(matrices)
+        self.orders = orders
+        t = BatchTune(*(tune or (0, 0, 0)))
+        h = ctypes.c_void_p()
+        check(load().pg_batch_plan_create(ptr(packed, ctypes.c_int64), ptr(offsets, ctypes.c_int64),
+                                          ptr(orders, ctypes.c_int32), self.count,
+                                          ctypes.byref(t), ctypes.byref(h)))
+        self._h = h
+        nt, nb, st, ext = ctypes.c_uint32(), ctypes.c_int(), ctypes.c_uint64(), ctypes.c_int()
+        check(load().pg_batch_plan_info(h, ctypes.byref(nt), ctypes.byref(nb), ctypes.byref(st),
+                                        ctypes.byref(ext)))
+        self.tasks, self.blocks, self.kernel_states, self.external = nt.value, nb.value, st.value, ext.value
+
+    def launch(self, stream: int | None = None) -> None:
+        check(load().pg_batch_plan_launch(self._h, ctypes.c_void_p(stream or 0)))
+
+    def results(self, stream: int | None = None) -> list[int]:
+        out = np.zeros(self.count * self.limbs, dtype=np.uint32)
+        check(load().pg_batch_plan_result(self._h, ctypes.c_void_p(stream or 0),
+                                          ptr(out, ctypes.c_uint32), self.limbs))
+        return [limbs_to_int(out[i * self.limbs:(i + 1) * self.limbs]) for i in range(self.count)]
+
+    def close(self) -> None:
+        if self._h:
+            load().pg_batch_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def batch_exact(matrices) -> list[int]:
+    """One-shot host-to-host batched evaluation (pg_batch_exact)."""
+    limbs = batch_limbs(matrices)
+    packed, offsets, orders = pack_batch(matrices)
+    out = np.zeros(len(matrices) * limbs, dtype=np.uint32)
+    check(load().pg_batch_exact(ptr(packed, ctypes.c_int64), ptr(offsets, ctypes.c_int64),
+                                ptr(orders, ctypes.c_int32), len(matrices),
+                                ptr(out, ctypes.c_uint32), limbs))
+    return [limbs_to_int(out[i * limbs:(i + 1) * limbs]) for i in range(len(matrices))]
 
 
 def probe_int_throughput(variant: int, iters: int = 4096) -> float:
