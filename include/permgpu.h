@@ -152,6 +152,24 @@ int pg_batch_exact(const int64_t *A, const int64_t *offsets,
                    const int32_t *orders, int count, uint32_t *out, int limbs);
 
 /*
+ * pg_exact_permanent for callers that cannot allocate memory (no
+ * counterpart in the reference).  Code that runs during CUDA graph capture,
+ * plug-ins whose host owns every device allocation, and services that must
+ * not grow device memory after start-up cannot call cudaMalloc; this entry
+ * point allocates nothing (no device, pinned or host heap memory, no
+ * streams).  Its scratch is a fixed 32 KiB __device__ array inside the
+ * library, present on every GPU that loads it until exit; orders 2..48 fit
+ * and anything larger returns PG_ERANGE.  The caller passes the host matrix
+ * and the host output words; `stream` may be NULL (legacy default stream).
+ * All calls share the scratch: calls that overlap on the GPU race and must
+ * be serialised by the caller.  The first call on each device looks up the
+ * scratch address (cudaGetSymbolAddress) and should come before any stream
+ * capture.
+ */
+int pg_exact_permanent_noalloc(const int64_t *A, int n, uint32_t *out,
+                               int limbs, void *stream);
+
+/*
  * Integer-pipe throughput probe (roofline denominator; no reference
  * counterpart): variant 0 mad.lo.u32, 1 mad.wide.u32, 2 mad.hi.u32,
  * 3 add.u32; writes thread-instructions per second for the whole GPU.

@@ -67,6 +67,8 @@ SIGNATURES = {
                             _c_intp], ctypes.c_int),
     "pg_batch_plan_destroy": ([ctypes.c_void_p], None),
     "pg_batch_exact": ([_c_i64p, _c_i64p, _c_i32p, ctypes.c_int, _c_u32p, ctypes.c_int], ctypes.c_int),
+    "pg_exact_permanent_noalloc": ([_c_i64p, ctypes.c_int, _c_u32p, ctypes.c_int, ctypes.c_void_p],
+                                   ctypes.c_int),
 }
 
 

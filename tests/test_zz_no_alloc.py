@@ -1,0 +1,71 @@
+"""GPU test of pg_exact_permanent_noalloc, the entry point for callers that
+cannot allocate memory (code running under CUDA graph capture, plug-ins
+whose host owns all device allocations, services with a fixed memory
+budget).  It must give exactly what the allocating entry point
+pg_exact_permanent gives — integers, so the tolerance is zero — on two
+calls in a row (the shared scratch keeps the previous call's contents and
+must be re-zeroed), and reject problems beyond its 32 KiB scratch.
+
+Collected last (file name) so a failure here never hides the other tests;
+it passes alone in a fresh process as well as after them.
+"""
+
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+PG_OK, PG_ERANGE, PG_EOVERFLOW = 0, 2, 7
+
+
+def _call(fn, a, limbs, *extra):
+    a = np.ascontiguousarray(a, dtype=np.int64)
+    out = np.zeros(limbs, dtype=np.uint32)
+    st = fn(a.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), a.shape[0],
+            out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), limbs, *extra)
+    return st, out
+
+
+def _lib():
+    from permgpu import _lib
+    handle = _lib.load()
+    assert handle.pg_cuda_runtime_available() == 1
+    return _lib, handle
+
+
+@pytest.mark.parametrize("n,seed,low,high", [(12, 1, -8, 8), (24, 0, -8, 8), (28, 7, -3, 3),
+                                             (40, 300, 0, 1), (6, 2, -(1 << 20), 1 << 20)])
+def test_noalloc_matches_allocating_entry_point_twice(n, seed, low, high):
+    lib, h = _lib()
+    rng = np.random.default_rng(seed)
+    a = rng.integers(low, high + 1, (n, n), dtype=np.int64)
+    limbs = lib.exact_limbs(a)
+    st, want = _call(h.pg_exact_permanent, a, limbs)
+    assert st == PG_OK, h.pg_last_error()
+    for _ in range(2):
+        st, got = _call(h.pg_exact_permanent_noalloc, a, limbs, None)
+        assert st == PG_OK, h.pg_last_error()
+        assert got.tolist() == want.tolist()
+
+
+def test_noalloc_alternating_matrices_do_not_leak_state():
+    lib, h = _lib()
+    rng = np.random.default_rng(9)
+    mats = [rng.integers(-8, 9, (20, 20), dtype=np.int64), rng.integers(-2, 3, (16, 16), dtype=np.int64)]
+    want = [lib.exact_permanent(m, lib.exact_limbs(m)) for m in mats]
+    for _ in range(2):
+        for m, w in zip(mats, want):
+            st, got = _call(h.pg_exact_permanent_noalloc, m, lib.exact_limbs(m), None)
+            assert st == PG_OK
+            assert lib.limbs_to_int(got) == w
+
+
+def test_noalloc_rejects_beyond_its_limits():
+    lib, h = _lib()
+    st, _ = _call(h.pg_exact_permanent_noalloc, np.ones((49, 49), np.int64), 16, None)
+    assert st == PG_ERANGE
+    assert b"2 <= n <= 48" in h.pg_last_error()
+    st, _ = _call(h.pg_exact_permanent_noalloc, np.full((5, 5), 1 << 40, np.int64), 16, None)
+    assert st == PG_EOVERFLOW
