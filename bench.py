@@ -427,13 +427,94 @@ def run_gpu_batch(args, world, rank, local):
     plan.close()
 
 
+def run_gpu_float28(args, world, rank, local):
+    """float28: 256 float64 matrices 28x28, entries N(0, 1/28), seed 5 (+rank);
+    one step = forward + hand-written gradient of the whole batch;
+    value = Glynn states per second (256 * 2^27 per step)."""
+    import numpy as np
+    import torch
+    from permgpu import workloads
+    from permgpu.f64 import permanent_f64
+
+    torch.cuda.set_device(local)
+    A_host = workloads.float28(seed=5 + 1000 * rank)
+    batch, n = A_host.shape[0], A_host.shape[1]
+    states = batch * (1 << (n - 1))
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    A = torch.from_numpy(A_host).cuda()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    for _ in range(args.warmup):
+        per, grad, s, gs = permanent_f64(A)
+    # accuracy against the oracle (forward, 2 matrices; gradient via the
+    # row-expansion identity sum_j a_ij g_ij = per for every row)
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    rel = []
+    for b in range(2):
+        want, _ = oracle.glynn_f64(A_host[b], os.cpu_count() or 1)
+        rel.append(abs(per[b].item() - want) / s[b].item())
+    g = grad.cpu().numpy()
+    exp_err = max(float(np.max(np.abs((A_host[b] * g[b]).sum(axis=1) - per[b].item())
+                               / (np.abs(A_host[b]) * gs[b].cpu().numpy()[:, None]).sum(axis=1)))
+                  for b in range(batch))
+    clocks = ClockSampler(local).start()
+    barrier(world)
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(args.steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        permanent_f64(A)
+        e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    torch.cuda.synchronize()
+    barrier(world)
+    e2e = []
+    pinned = torch.from_numpy(A_host).pin_memory()
+    for _ in range(max(1, args.steps // 2)):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        Ad = pinned.cuda(non_blocking=True)
+        p, gr, _, _ = permanent_f64(Ad)
+        p_host, g_host = p.cpu(), gr.cpu()
+        e2e.append(time.perf_counter() - t)
+    clk = clocks.stop()
+    step_ms = max_over_ranks(world, statistics.mean(ms))
+    e2e_s = max_over_ranks(world, statistics.mean(e2e))
+    if rank == 0:
+        print(json.dumps({
+            "metric": "FP64 Glynn forward+gradient steps/s (256 x 28x28)",
+            "value": world * states / (step_ms * 1e-3), "unit": "steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64 (double-float on FP32 pipes, FP64 re-initialisation and Kahan flushes)",
+            "data": "synthetic",
+            "config": {"workload": "float28: 256 float64 matrices 28x28, entries N(0,1/28), "
+                                   "numpy default_rng(5)", "states": states,
+                       "l2": "flushed between timed steps (256 MiB write)"},
+            "max_rel_err_forward_vs_oracle": max(rel),
+            "max_rel_err_row_expansion": exp_err,
+            "tolerance": 1e-10,
+            "e2e": {"value": world * states / e2e_s, "unit": "steps/s",
+                    "h2d_bytes_per_step": int(A_host.nbytes),
+                    "d2h_bytes_per_step": int(batch * 8 + A_host.nbytes),
+                    "ms_per_step": 1e3 * e2e_s},
+            "clocks": clk, "gpu_launches": 2 * args.steps,
+        }))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="generic32", choices=sorted(WORKLOADS) + ["batch4096"])
+    ap.add_argument("--workload", default="generic32",
+                    choices=sorted(WORKLOADS) + ["batch4096", "float28"])
     ap.add_argument("--residue-loop-sample", type=int, default=256)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -443,6 +524,8 @@ def main():
         run_reference(args, world, rank)
     elif args.workload == "batch4096":
         run_gpu_batch(args, world, rank, local)
+    elif args.workload == "float28":
+        run_gpu_float28(args, world, rank, local)
     else:
         run_gpu(args, world, rank, local)
     if world > 1:

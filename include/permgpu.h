@@ -152,6 +152,22 @@ int pg_batch_exact(const int64_t *A, const int64_t *offsets,
                    const int32_t *orders, int count, uint32_t *out, int limbs);
 
 /*
+ * FP64 Glynn permanent and gradient for a batch of real matrices, device
+ * pointers (torch tensors) on `stream` (NULL: the library's stream):
+ *   per[b]          = per(A_b)                       (A: [batch][n][n] f64)
+ *   grad[b][i][j]   = d per / d a_ij = per(A_b without row i, column j)
+ *   abs_sum[b]      = 2^(1-n) sum |terms|  (error scale of per[b])
+ *   grad_abs[b][i]  = 2^(1-n) sum |prod_{l != i} s_l|  (scale of row i)
+ * grad / abs_sum / grad_abs may be NULL (grad NULL: forward only).
+ * 2 <= n <= 32.  Replaces permanent_parallel_real (perm_parallel_cuda.cu:
+ * 343-414, forward only, one matrix); the gradient has no reference
+ * counterpart.  Synchronises `stream` before returning.
+ */
+int pg_glynn_f64_dev(const double *A, int batch, int n, double *per,
+                     double *grad, double *abs_sum, double *grad_abs,
+                     void *stream);
+
+/*
  * pg_exact_permanent for callers that cannot allocate memory (no
  * counterpart in the reference).  Code that runs during CUDA graph capture,
  * plug-ins whose host owns every device allocation, and services that must

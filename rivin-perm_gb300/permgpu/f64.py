@@ -1,0 +1,144 @@
+"""Differentiable FP64 permanent (Glynn) on the GPU.
+
+    GlynnPermanent.apply(A)      A: (..., n, n) float64 CUDA tensor -> (...)
+    permanent_f64(A)             forward (+ gradient) with error scales
+    permanent_float(A)           numpy API of rivin-perm perm_float.permanent_float
+                                 (perm_float.py:353-370), real matrices
+    permanent_gpu(A)             numpy API of perm_parallel.permanent_gpu
+                                 (perm_parallel.py:104-164), real matrices
+
+The forward and the gradient d per / d a_ij = per(A without row i, column j)
+come out of one Glynn traversal (pg_glynn_f64_dev).  The backward of the
+autograd Function is the hand-written gradient from that traversal, scaled
+by the incoming gradient.  Every result carries the sum of |terms| it was
+accumulated from (scaled by 2^(1-n)), the scale against which its relative
+error is stated.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from typing import Optional, Tuple
+
+import numpy as np
+
+from . import _lib
+
+def _fn():
+    return _lib.load().pg_glynn_f64_dev
+
+
+def permanent_f64(A, want_grad: bool = True):
+    """(per, grad, abs_sum, grad_abs) for a (batch, n, n) float64 CUDA tensor.
+
+    grad / grad_abs are None when want_grad is False.  grad_abs[b, i] is the
+    error scale of row i of the gradient (sum over states of |prod_{l != i}
+    s_l|, times 2^(1-n)).
+    """
+    import torch
+    if A.dtype != torch.float64 or not A.is_cuda:
+        raise TypeError("A must be a float64 CUDA tensor")
+    if A.dim() < 2 or A.shape[-1] != A.shape[-2]:
+        raise ValueError("A must have shape (..., n, n)")
+    lead = A.shape[:-2]
+    n = A.shape[-1]
+    Ab = A.reshape(-1, n, n).contiguous()
+    batch = Ab.shape[0]
+    per = torch.empty(batch, dtype=torch.float64, device=A.device)
+    abs_sum = torch.empty_like(per)
+    grad = grad_abs = None
+    if n == 0:
+        per.fill_(1.0)
+        abs_sum.fill_(1.0)
+        if want_grad:
+            grad = torch.zeros_like(Ab)
+            grad_abs = torch.zeros(batch, 0, dtype=torch.float64, device=A.device)
+    elif n == 1:
+        per.copy_(Ab[:, 0, 0])
+        abs_sum.copy_(Ab[:, 0, 0].abs())
+        if want_grad:
+            grad = torch.ones_like(Ab)
+            grad_abs = torch.ones(batch, 1, dtype=torch.float64, device=A.device)
+    elif batch:
+        if want_grad:
+            grad = torch.empty_like(Ab)
+            grad_abs = torch.empty(batch, n, dtype=torch.float64, device=A.device)
+        stream = torch.cuda.current_stream(A.device).cuda_stream
+        _lib.check(_fn()(Ab.data_ptr(), batch, n, per.data_ptr(),
+                         grad.data_ptr() if want_grad else None, abs_sum.data_ptr(),
+                         grad_abs.data_ptr() if want_grad else None, stream or None))
+    per = per.reshape(lead)
+    abs_sum = abs_sum.reshape(lead)
+    if want_grad:
+        grad = grad.reshape(A.shape)
+        grad_abs = grad_abs.reshape(*lead, n)
+    return per, grad, abs_sum, grad_abs
+
+
+def _function():
+    import torch
+
+    class GlynnPermanent(torch.autograd.Function):
+        """per(A) over the last two dimensions, FP64, with the hand-written
+        Glynn gradient computed in the same GPU traversal as the forward."""
+
+        @staticmethod
+        def forward(ctx, A):
+            need = ctx.needs_input_grad[0]
+            per, grad, _, _ = permanent_f64(A.detach(), want_grad=need)
+            if need:
+                ctx.save_for_backward(grad)
+            return per
+
+        @staticmethod
+        def backward(ctx, grad_out):
+            (grad,) = ctx.saved_tensors
+            return grad_out[..., None, None] * grad
+
+    return GlynnPermanent
+
+
+_GLYNN = None
+
+
+def glynn_permanent(A):
+    """Differentiable per(A) (autograd Function)."""
+    global _GLYNN
+    if _GLYNN is None:
+        _GLYNN = _function()
+    return _GLYNN.apply(A)
+
+
+def __getattr__(name):
+    if name == "GlynnPermanent":
+        global _GLYNN
+        if _GLYNN is None:
+            _GLYNN = _function()
+        return _GLYNN
+    raise AttributeError(name)
+
+
+def permanent_float(matrix) -> float:
+    """perm_float.permanent_float API for a real square matrix (FP64)."""
+    import torch
+    a = np.asarray(matrix)
+    if np.iscomplexobj(a):
+        raise TypeError("complex matrices are not supported by the GPU FP64 engine")
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if a.ndim != 2 or a.shape[0] != a.shape[1]:
+        raise ValueError("Expected a square 2-D matrix")
+    t = torch.from_numpy(a).cuda()
+    per, _, _, _ = permanent_f64(t[None], want_grad=False)
+    return float(per[0].item())
+
+
+def permanent_gpu(matrix, real: Optional[bool] = None) -> float:
+    """perm_parallel.permanent_gpu API (real matrices)."""
+    a = np.asarray(matrix)
+    if real is False or np.iscomplexobj(a):
+        raise TypeError("complex matrices are not supported by the GPU FP64 engine")
+    if a.ndim != 2 or a.shape[0] != a.shape[1]:
+        raise ValueError(f"Expected a square 2-D matrix, got shape {a.shape}")
+    if a.shape[0] == 0:
+        return 1.0
+    return permanent_float(a)

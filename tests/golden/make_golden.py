@@ -181,7 +181,7 @@ def main():
         fl.append({"matrix": a.tolist(), "permanent": float(perm_float.permanent_float(a))})
     dump("float_small.json", {"source": "perm_float.permanent_float (Ryser + Kahan)", "cases": fl})
 
-    if args.slow:
+    if args.slow and not (HERE / "exact_generic32.json").exists():
         a = workloads.generic32()
         t = time.time()
         v = perm.matrix_permanent(a.tolist(), method="generic")
@@ -189,7 +189,8 @@ def main():
                                       "permanent": str(v), "workload": "generic32",
                                       "cpu_seconds": round(time.time() - t, 1),
                                       "source": "perm.matrix_permanent(A, method='generic')"})
-        mats = workloads.float20int(1)
+    if args.slow:
+        mats = workloads.float20int(2)
         out = []
         for a in mats:
             ai = a.astype(int).tolist()
@@ -199,7 +200,7 @@ def main():
                                                method="generic")) for j in range(n)] for i in range(n)]
             out.append({"matrix": ai, "permanent": str(per), "minors": grad})
         dump("float20int_minors.json", {"source": "perm.matrix_permanent on A and every minor",
-                                        "generator": "permgpu.workloads.float20int(1)",
+                                        "generator": "permgpu.workloads.float20int(2)",
                                         "cases": out})
 
 

@@ -101,3 +101,16 @@ def test_schur_table_small_orders_from_oracle_crt():
         if x > bound:
             x -= math.prod(moduli)
         assert x == int(table[str(n)])
+
+
+def test_float_gradient_oracle_matches_reference_minors():
+    # integer-valued 20x20: the reference's exact permanents of all 400
+    # minors (perm.matrix_permanent) are the gradient
+    data = golden("float20int_minors.json")
+    c = data["cases"][0]
+    a = np.array(c["matrix"], dtype=np.float64)
+    g = oracle.glynn_f64_grad(a, 8)
+    want = np.array([[float(int(x)) for x in row] for row in c["minors"]])
+    assert np.array_equal(g, want)
+    v, _ = oracle.glynn_f64(a, 8)
+    assert v == float(int(c["permanent"]))
