@@ -507,6 +507,69 @@ def run_gpu_float28(args, world, rank, local):
         }))
 
 
+def run_gpu_exact_set(args, world, rank, local):
+    """schur: exact perm(S_31) and perm(S_33) (residue engine, primes == 1 mod
+    n, below 2^31, Graham-Lehmer congruence at CRT time); binary40: eight
+    40x40 Bernoulli(0.5) 0/1 matrices (seeds 300..307) through the binary
+    API (matching blocks, exact engine).  One step = the whole set; value =
+    Glynn steps per second (minor / block states, times primes for Schur)."""
+    import numpy as np
+    import torch
+    import permgpu
+    from permgpu import workloads
+    from permgpu.crt import plan_schur
+    torch.cuda.set_device(local)
+    table = json.loads((ROOT / "tests" / "golden" / "schur.json").read_text())["table"]
+    if args.workload == "schur":
+        items = [31, 33]
+        states = sum(len(plan_schur(n)[0]) * (1 << (n - 2)) for n in items)
+
+        def step():
+            return [permgpu.permanent(n) for n in items]
+        want = [int(table[str(n)]) for n in items]
+        desc = "perm(S_31), perm(S_33): (n-1)x(n-1) minors, primes == 1 (mod n) < 2^31"
+    else:
+        mats = workloads.binary40(8)
+        items = [m.tolist() for m in mats]
+        states = len(items) * (1 << 39)
+
+        def step():
+            return [permgpu.binary_permanent(m) for m in items]
+        want = None
+        desc = "eight 40x40 Bernoulli(0.5) 0/1 matrices, numpy default_rng(300..307)"
+    for _ in range(args.warmup):
+        got = step()
+    if want is not None and got != want:
+        raise SystemExit(f"parity failure: {got} != {want}")
+    clocks = ClockSampler(local).start()
+    barrier(world)
+    ts = []
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        res = step()
+        ts.append(time.perf_counter() - t)
+        if res != got:
+            raise SystemExit("results changed between steps")
+    barrier(world)
+    clk = clocks.stop()
+    step_s = max_over_ranks(world, statistics.mean(ts))
+    if rank == 0:
+        print(json.dumps({
+            "metric": f"Glynn steps/s ({args.workload})", "value": world * states / step_s,
+            "unit": "steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * step_s, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+            "config": {"workload": f"{args.workload}: {desc}", "states": states},
+            "time_to_exact_s": step_s, "results": [str(v) for v in got],
+            "result_checked_against_reference": want is not None,
+            "e2e": {"value": world * states / step_s, "unit": "steps/s",
+                    "h2d_bytes_per_step": None, "d2h_bytes_per_step": None,
+                    "note": "whole-call API timed end to end (host inputs, host results)"},
+            "clocks": clk,
+        }))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -514,7 +577,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="generic32",
-                    choices=sorted(WORKLOADS) + ["batch4096", "float28"])
+                    choices=sorted(WORKLOADS) + ["batch4096", "float28", "schur", "binary40"])
     ap.add_argument("--residue-loop-sample", type=int, default=256)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -526,6 +589,8 @@ def main():
         run_gpu_batch(args, world, rank, local)
     elif args.workload == "float28":
         run_gpu_float28(args, world, rank, local)
+    elif args.workload in ("schur", "binary40"):
+        run_gpu_exact_set(args, world, rank, local)
     else:
         run_gpu(args, world, rank, local)
     if world > 1:

@@ -100,6 +100,19 @@ int pg_exact_permanent(const int64_t *A, int n, uint32_t *out, int limbs);
 int pg_exact_supported(const int64_t *A, int n);
 
 /*
+ * Sharded exact evaluation: the unscaled Glynn sum over Gray states
+ * [state_lo, state_hi) (multiples of 4) as *nwords 64-bit words, word w of
+ * weight 2^(32 w), the last word signed.  Summing the words of a partition
+ * of [0, 2^(n-1)) over ranks/hosts and dividing by 2^(n-1) gives per(A).
+ * Same matrix contract as pg_exact_permanent; mirrors the contiguous
+ * Gray-block split of perm_c_omp.c:565-603 across devices instead of
+ * threads.
+ */
+int pg_exact_partial(const int64_t *A, int n, uint64_t state_lo,
+                     uint64_t state_hi, int64_t *words, int max_words,
+                     int *nwords);
+
+/*
  * Reusable exact plan: the host work of pg_exact_permanent (grouping, column
  * tables, launch shape) done once and the tables kept resident in device
  * memory, so repeated evaluations pay only the launch.  `stream` may be NULL

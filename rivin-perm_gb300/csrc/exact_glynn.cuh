@@ -192,8 +192,9 @@ struct ExactArgs {
     unsigned long long *acc;   // [NL] per-word sums (two's complement, zeroed)
     int *status;
     volatile const int *abort_flag;
-    uint64_t chunks;
+    uint64_t chunks;           // chunks to walk: [chunk0, chunk0 + chunks)
     int log_len;               // >= LOGU, <= 30
+    uint64_t chunk0;           // first chunk (0 for a whole traversal)
 };
 
 // Resident blocks per SM requested from ptxas: a register budget of about
@@ -224,8 +225,8 @@ exact_glynn_kernel(ExactArgs a) {
     // one contiguous, balanced range of chunks per thread
     const uint64_t T = (uint64_t)gridDim.x * blockDim.x;
     const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const uint64_t c_begin = tid * a.chunks / T;
-    const uint64_t c_end = (tid + 1) * a.chunks / T;
+    const uint64_t c_begin = a.chunk0 + tid * a.chunks / T;
+    const uint64_t c_end = a.chunk0 + (tid + 1) * a.chunks / T;
     bool aborted = false;
     if (c_begin < c_end) {
         int32_t s[N];

@@ -98,6 +98,7 @@ static void add_i64_at(std::vector<uint32_t> &w, int pos, long long v) {
 struct ExactPlan {
     int n = 0, G = 0, NG = 0, NL = 0, need_bits = 0;
     ChunkPlan chunks{};
+    uint64_t chunk0 = 0;
     uint64_t blocks = 0;
     size_t off_acc = 0, off_status = 0, total = 0;
     std::vector<char> image;     // host image of [tab | init | acc | status]
@@ -179,8 +180,25 @@ static int plan_launch(ExactPlan *P, cudaStream_t stream) {
     args.abort_flag = P->abort_dev;
     args.chunks = P->chunks.chunks;
     args.log_len = P->chunks.log_len;
+    args.chunk0 = P->chunk0;
     PG_CUDA(cudaMemsetAsync(P->dev + P->off_acc, 0, P->total - P->off_acc, stream));
     PG_CUDA(launch_exact_any(P->n, P->G, args, (int)P->blocks, stream));
+    return PG_OK;
+}
+
+// Restrict a built plan to Gray states [lo, hi): both must be multiples of
+// 4 (the kernel's two-step unroll keeps chunk starts even and aligned).
+static int plan_restrict(ExactPlan *P, uint64_t lo, uint64_t hi) {
+    const uint64_t states = 1ull << (P->n - 1);
+    if (lo >= hi || hi > states) return fail(PG_ERANGE, "state range must satisfy lo < hi <= 2^(n-1)");
+    int ll = P->chunks.log_len;
+    while (ll > 0 && (((lo | hi) & ((1ull << ll) - 1)) != 0)) ll--;
+    const int logu = (P->n - 1) < EXACT_LOGU ? (P->n - 1) : EXACT_LOGU;
+    if (ll < logu || ll < 1)
+        return fail(PG_EINVAL, "state range bounds must be multiples of 4");
+    P->chunks.log_len = ll;
+    P->chunk0 = lo >> ll;
+    P->chunks.chunks = (hi - lo) >> ll;
     return PG_OK;
 }
 
@@ -259,6 +277,32 @@ int pg_exact_permanent(const int64_t *A, int n, uint32_t *out, int limbs) {
         return PG_OK;
     }
     return exact_run(A, n, out, limbs);
+}
+
+int pg_exact_partial(const int64_t *A, int n, uint64_t state_lo, uint64_t state_hi,
+                     int64_t *words, int max_words, int *nwords) {
+    using namespace pg;
+    if (!A || !words || !nwords || n < 2 || n >= 64) return fail(PG_EINVAL, "bad arguments");
+    ExactPlan P;
+    int st = plan_build(A, n, &P);
+    if (st != PG_OK) return st;
+    if ((st = plan_restrict(&P, state_lo, state_hi)) != PG_OK) return st;
+    if (max_words < P.NL) return fail(PG_ERANGE, "words buffer too small");
+    Workspace *ws;
+    st = workspace(&ws, P.total, P.total);
+    if (st != PG_OK) return st;
+    P.dev = (char *)ws->dev;
+    P.host = (char *)ws->host;
+    P.stream = ws->stream;
+    if ((st = plan_upload(&P)) != PG_OK) return st;
+    if ((st = plan_launch(&P, P.stream)) != PG_OK) return st;
+    PG_CUDA(cudaMemcpyAsync(P.host + P.off_acc, P.dev + P.off_acc, P.total - P.off_acc,
+                            cudaMemcpyDeviceToHost, P.stream));
+    PG_CUDA(cudaStreamSynchronize(P.stream));
+    if (*(int *)(P.host + P.off_status)) return fail(PG_EABORT, "aborted by pg_abort()");
+    std::memcpy(words, P.host + P.off_acc, (size_t)P.NL * 8);
+    *nwords = P.NL;
+    return PG_OK;
 }
 
 int pg_exact_plan_create(const int64_t *A, int n, pg_exact_plan **out) {

@@ -182,6 +182,7 @@ extern "C" int pg_exact_permanent_noalloc(const int64_t *A, int n, uint32_t *out
     args.abort_flag = (volatile const int *)(scratch + off_zero);
     args.chunks = 1ull << (log_states - log_len);
     args.log_len = log_len;
+    args.chunk0 = 0;
     PG_CUDA(launch_exact_any(n, G, args, (int)blocks, s));
 
     long long acc[64];          // NL <= 18 for every compiled shape

@@ -69,6 +69,8 @@ SIGNATURES = {
     "pg_batch_exact": ([_c_i64p, _c_i64p, _c_i32p, ctypes.c_int, _c_u32p, ctypes.c_int], ctypes.c_int),
     "pg_exact_permanent_noalloc": ([_c_i64p, ctypes.c_int, _c_u32p, ctypes.c_int, ctypes.c_void_p],
                                    ctypes.c_int),
+    "pg_exact_partial": ([_c_i64p, ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64, _c_i64p,
+                          ctypes.c_int, _c_intp], ctypes.c_int),
     "pg_glynn_f64_dev": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
 }

@@ -42,8 +42,10 @@ def permanent_f64(A, want_grad: bool = True):
         raise ValueError("A must have shape (..., n, n)")
     lead = A.shape[:-2]
     n = A.shape[-1]
-    Ab = A.reshape(-1, n, n).contiguous()
-    batch = Ab.shape[0]
+    batch = 1
+    for d in lead:
+        batch *= int(d)
+    Ab = A.reshape(batch, n, n).contiguous()
     per = torch.empty(batch, dtype=torch.float64, device=A.device)
     abs_sum = torch.empty_like(per)
     grad = grad_abs = None

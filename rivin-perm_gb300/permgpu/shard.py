@@ -1,0 +1,70 @@
+"""Sharding one permanent across ranks / hosts.
+
+The Glynn sum is a sum over 2^(n-1) independent Gray states, so any
+partition of the state range into contiguous pieces gives partial sums that
+simply add: per(A) = 2^(1-n) * sum_ranks S_rank.  There is no device
+collective: each rank evaluates its range (pg_exact_partial on its GPU),
+and the exchange is a host-level gather of a few 64-bit words per rank.
+
+    lo, hi = state_range(n, rank, world)
+    words = exact_partial_words(A, lo, hi)          # on the rank's GPU
+    all = gather(words)                              # any transport
+    per = combine_exact_words(all, n)
+
+The same split works for residues (combine_residues).
+"""
+
+from __future__ import annotations
+
+import ctypes
+from typing import Iterable, List, Sequence, Tuple
+
+import numpy as np
+
+from . import _lib
+
+
+def state_range(n: int, rank: int, world: int, align: int = 64) -> Tuple[int, int]:
+    """Contiguous, balanced slice [lo, hi) of the 2^(n-1) Gray states for
+    `rank` of `world`, with boundaries on multiples of `align` (a power of
+    two) so every slice is a whole number of aligned chunks."""
+    states = 1 << max(n - 1, 0)
+    if world < 1 or not 0 <= rank < world:
+        raise ValueError("bad rank/world")
+    align = min(align, states)
+    units = states // align
+    lo = rank * units // world * align
+    hi = (rank + 1) * units // world * align
+    return lo, hi
+
+
+def exact_partial_words(matrix, lo: int, hi: int) -> List[int]:
+    """Unscaled per-word sums of the Glynn terms over states [lo, hi) from
+    the exact GPU engine (word w has weight 2^(32 w), last word signed)."""
+    a = np.ascontiguousarray(matrix, dtype=np.int64)
+    out = np.zeros(32, dtype=np.int64)
+    nw = ctypes.c_int()
+    _lib.check(_lib.load().pg_exact_partial(_lib.ptr(a, ctypes.c_int64), a.shape[0],
+                                            ctypes.c_uint64(lo), ctypes.c_uint64(hi),
+                                            _lib.ptr(out, ctypes.c_int64), 32,
+                                            ctypes.byref(nw)))
+    return [int(x) for x in out[: nw.value]]
+
+
+def words_value(words: Sequence[int]) -> int:
+    return sum(int(w) << (32 * i) for i, w in enumerate(words))
+
+
+def combine_exact_words(word_lists: Iterable[Sequence[int]], n: int) -> int:
+    """per(A) from the ranks' partial words (checks 2^(n-1) divides the sum)."""
+    total = sum(words_value(w) for w in word_lists)
+    if n >= 1 and total % (1 << (n - 1)):
+        raise RuntimeError("partial sums do not add up to a multiple of 2^(n-1)")
+    return total >> max(n - 1, 0)
+
+
+def combine_residues(partials: Iterable[int], p: int, n: int) -> int:
+    """per(A) mod odd p from unscaled partial Glynn sums mod p."""
+    total = sum(int(x) for x in partials) % p
+    inv2 = (p + 1) // 2
+    return total * pow(inv2, n - 1, p) % p

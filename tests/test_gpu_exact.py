@@ -95,3 +95,12 @@ def test_binary_residue_path_equals_exact_path(lib):
     exact = permgpu.binary_permanent(m.tolist())
     primes = binary_primes_above(binary_block_bound(m.tolist()))
     assert lib.binary_residues(m, primes) == [exact % p for p in primes]
+
+
+@pytest.mark.parametrize("world", [1, 2, 3, 8])
+def test_sharded_partials_combine_to_exact(lib, world):
+    from permgpu import shard, workloads
+    a = workloads.generic_matrix(24, 0)
+    want = int(golden("exact_generic.json")["cases"][-1]["permanent"])
+    words = [shard.exact_partial_words(a, *shard.state_range(24, r, world)) for r in range(world)]
+    assert shard.combine_exact_words(words, 24) == want
