@@ -437,7 +437,7 @@ def run_gpu_float28(args, world, rank, local):
     from permgpu.f64 import permanent_f64
 
     torch.cuda.set_device(local)
-    A_host = workloads.float28(seed=5 + 1000 * rank)
+    A_host = workloads.float28(count=args.batch, seed=5 + 1000 * rank)
     batch, n = A_host.shape[0], A_host.shape[1]
     states = batch * (1 << (n - 1))
     stream = torch.cuda.Stream()
@@ -581,6 +581,8 @@ def main():
     ap.add_argument("--residue-loop-sample", type=int, default=256)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--batch", type=int, default=256,
+                    help="float28: matrices per step (256 is the workload; smaller for profiling)")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":
