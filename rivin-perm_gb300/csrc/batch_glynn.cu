@@ -19,7 +19,6 @@
 
 #include <algorithm>
 #include <cmath>
-#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -314,10 +313,7 @@ int pg_batch_plan_create(const int64_t *A, const int64_t *offsets, const int32_t
     }
     // float rows when every in-kernel row bound is < 2^11 (tables hold small
     // integers, exactly representable as floats)
-    {
-        const char *rows_env = std::getenv("PERMGPU_EXACT_ROWS");
-        P.fp = rows_env && std::strcmp(rows_env, "float") == 0 && batch_max_bound < 2048;
-    }
+    P.fp = batch_max_bound < 2048;
     if (P.fp)
         for (auto &w : tables) {
             const float f = (float)w;

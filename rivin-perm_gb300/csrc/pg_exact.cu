@@ -5,7 +5,6 @@
 
 #include <algorithm>
 #include <cmath>
-#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -71,20 +70,14 @@ static int choose_group(const int64_t *A, int n, std::vector<int> *order,
         B[i] = (uint64_t)s;
         if (B[i] > maxB) maxB = B[i];
     }
-    // PERMGPU_EXACT_ROWS=int|float and PERMGPU_EXACT_ZSKIP=0|1 override the
-    // choice (for measuring the variants against each other)
-    const char *rows_env = std::getenv("PERMGPU_EXACT_ROWS");
-    const char *zs_env = std::getenv("PERMGPU_EXACT_ZSKIP");
-    bool want_fp = false;
-    if (rows_env && std::strcmp(rows_env, "float") == 0) want_fp = maxB < 2048;
-    const bool want_zskip = zs_env ? std::atoi(zs_env) != 0 : binary;
+    const bool want_fp = maxB < 2048;
     for (int pass = want_fp ? 0 : 1; pass < 2; pass++) {
         const bool f = pass == 0;
         for (int G = 6; G >= 1; G--) {
             if (!exact_compiled(n, G, f)) continue;
             if (group_rows(B, n, G, order)) {
                 if (fp) *fp = f;
-                if (zskip) *zskip = want_zskip;
+                if (zskip) *zskip = binary;
                 return G;
             }
         }
