@@ -51,11 +51,9 @@ struct BatchArgs {
     volatile const int *abort_flag;
 };
 
-template <int N, bool FP>
-__device__ __forceinline__ void batch_task(const int32_t *wtab_words, const BatchArgs &a,
+template <int N>
+__device__ __forceinline__ void batch_task(const int32_t *wtab, const BatchArgs &a,
                                            const BatchTask &t, int lane) {
-    using T = typename std::conditional<FP, float, int32_t>::type;
-    const T *wtab = reinterpret_cast<const T *>(wtab_words);
     constexpr int G = N >= 4 ? 4 : N;
     using S = ExactShape<N, G>;
     constexpr int NP = S::NP, NL = S::NL;
@@ -72,9 +70,9 @@ __device__ __forceinline__ void batch_task(const int32_t *wtab_words, const Batc
     for (int l = 0; l < NL; l++) acc[l] = 0;
     bool ok = true;
     if (cb < ce) {
-        T s[N];
-        exact_init<N, T>(wtab, wtab + (N - 1) * 2 * NP, s, cb << log_len);
-        ok = exact_walk<N, G, T>(wtab, s, acc, cb, ce, log_len, a.abort_flag, false);
+        int32_t s[N];
+        exact_init<N>(wtab, wtab + (N - 1) * 2 * NP, s, cb << log_len);
+        ok = exact_walk<N, G>(wtab, s, acc, cb, ce, log_len, a.abort_flag);
     }
     if (!ok) atomicExch(a.status, 1);
 #pragma unroll
@@ -87,7 +85,6 @@ __device__ __forceinline__ void batch_task(const int32_t *wtab_words, const Batc
     }
 }
 
-template <bool FP>
 __global__ void __launch_bounds__(256, 2) batch_glynn_kernel(BatchArgs a) {
     extern __shared__ int4 bsmem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -110,7 +107,7 @@ __global__ void __launch_bounds__(256, 2) batch_glynn_kernel(BatchArgs a) {
             cur = t.m;
         }
         switch (n) {
-#define PG_BATCH_CASE(NN) case NN: batch_task<NN, FP>(wtab, a, t, lane); break;
+#define PG_BATCH_CASE(NN) case NN: batch_task<NN>(wtab, a, t, lane); break;
             PG_BATCH_CASE(2) PG_BATCH_CASE(3) PG_BATCH_CASE(4) PG_BATCH_CASE(5)
             PG_BATCH_CASE(6) PG_BATCH_CASE(7) PG_BATCH_CASE(8) PG_BATCH_CASE(9)
             PG_BATCH_CASE(10) PG_BATCH_CASE(11) PG_BATCH_CASE(12) PG_BATCH_CASE(13)
@@ -139,19 +136,6 @@ static void add_i64_at(std::vector<uint32_t> &w, int pos, long long v) {
         w[i] = (uint32_t)t;
         carry = t >> 32;
     }
-}
-
-static uint64_t max_row_bound(const int64_t *A, int n) {
-    uint64_t mx = 0;
-    for (int i = 0; i < n; i++) {
-        unsigned __int128 s = 0;
-        for (int j = 0; j < n; j++) {
-            const int64_t v = A[(size_t)i * n + j];
-            s += v < 0 ? (unsigned __int128)(-(__int128)v) : (unsigned __int128)v;
-        }
-        if (s > mx) mx = s > ~0ull ? ~0ull : (uint64_t)s;
-    }
-    return mx;
 }
 
 // Row order for groups of 4 (every group's bound product < 2^31), or false.
@@ -207,7 +191,6 @@ struct BatchPlan {
     size_t total = 0, off_acc = 0, off_counter = 0, off_status = 0;
     uint32_t ntasks = 0;
     int blocks = 0;
-    bool fp = false;
     size_t smem = 0;
     char *dev = nullptr;
     char *host = nullptr;
@@ -253,7 +236,6 @@ int pg_batch_plan_create(const int64_t *A, const int64_t *offsets, const int32_t
     P.bound_bits.assign(count, 0.0);
 
     std::vector<int32_t> tables;
-    uint64_t batch_max_bound = 0;
     std::vector<uint64_t> toff(count, 0), nchunks(count, 0);
     std::vector<uint8_t> ord8(count, 0), loglen(count, 0);
     std::vector<BatchTask> tasks;
@@ -276,7 +258,6 @@ int pg_batch_plan_create(const int64_t *A, const int64_t *offsets, const int32_t
             continue;
         }
         P.in_kernel[m] = 1;
-        batch_max_bound = std::max(batch_max_bound, max_row_bound(a, n));
         const int NP = (n + 3) & ~3;
         toff[m] = tables.size();
         const size_t base = tables.size();
@@ -311,14 +292,6 @@ int pg_batch_plan_create(const int64_t *A, const int64_t *offsets, const int32_t
             task_work.push_back(std::min<uint64_t>(k, span) * (1ull << ll) * (uint64_t)n);
         }
     }
-    // float rows when every in-kernel row bound is < 2^11 (tables hold small
-    // integers, exactly representable as floats)
-    P.fp = batch_max_bound < 2048;
-    if (P.fp)
-        for (auto &w : tables) {
-            const float f = (float)w;
-            std::memcpy(&w, &f, sizeof(f));
-        }
     // largest tasks first (LPT order); ties keep matrix order
     std::vector<uint32_t> idx(tasks.size());
     for (size_t i = 0; i < idx.size(); i++) idx[i] = (uint32_t)i;
@@ -377,11 +350,11 @@ int pg_batch_plan_create(const int64_t *A, const int64_t *offsets, const int32_t
     a.abort_flag = abort_dev;
 
     P.smem = (size_t)8 * BATCH_SLICE * sizeof(int32_t);
-    void (*kern)(BatchArgs) = P.fp ? batch_glynn_kernel<true> : batch_glynn_kernel<false>;
-    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.smem);
+    e = cudaFuncSetAttribute(batch_glynn_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)P.smem);
     int occ = 0;
     if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 256, P.smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_glynn_kernel, 256, P.smem);
     if (e != cudaSuccess) {
         st = cuda_fail(e, "batch kernel attributes");
         pg_batch_plan_destroy(h);
@@ -394,7 +367,7 @@ int pg_batch_plan_create(const int64_t *A, const int64_t *offsets, const int32_t
     if (e == cudaSuccess) {
         cudaMemsetAsync(P.dev + P.off_acc, 0, P.total - P.off_acc, P.stream);
         if (P.ntasks)
-            kern<<<P.blocks, 256, P.smem, P.stream>>>(a);
+            batch_glynn_kernel<<<P.blocks, 256, P.smem, P.stream>>>(a);
         e = cudaStreamEndCapture(P.stream, &P.graph);
     }
     if (e == cudaSuccess) e = cudaGraphInstantiate(&P.exec, P.graph, 0);

@@ -26,8 +26,6 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#include <type_traits>
-
 #include "acc_chain.cuh"
 #include "mp_mul.cuh"
 
@@ -84,32 +82,31 @@ struct ExactShape {
 };
 
 // Row sums of Gray state `start`: init - sum_{j in gray(start)} 2 a_j.
-// T is int32_t (general) or float (row bounds < 2^11: exact small integers).
-template <int N, typename T>
-__device__ __forceinline__ void exact_init(const T *tab, const T *init, T *s, uint64_t start) {
+template <int N>
+__device__ __forceinline__ void exact_init(const int32_t *tab, const int32_t *init,
+                                           int32_t *s, uint64_t start) {
     constexpr int NP = (N + 3) & ~3;
     const uint64_t gs = start ^ (start >> 1);
 #pragma unroll
     for (int i = 0; i < N; i++) s[i] = init[i];
     for (int j = 0; j < N - 1; j++) {
         if ((gs >> j) & 1) {
-            const T *col = tab + (2 * j + 1) * NP;
+            const int32_t *col = tab + (2 * j + 1) * NP;
 #pragma unroll
             for (int i = 0; i < N; i++) s[i] += col[i];
         }
     }
 }
 
-// |x| of an integer-valued float with |x| < 2^23 as an integer: adding 2^23
-// (with the |.| operand modifier) leaves exactly |x| in the mantissa bits.
-__device__ __forceinline__ uint32_t exact_fmag(float x) {
-    return __float_as_uint(fabsf(x) + 8388608.0f) & 0x7fffffu;
-}
-
-// Group magnitudes and the sign word of one term.
+// One Glynn term at the current row sums: acc += (-1)^(odd + signs) * prod s.
 template <int N, int G>
-__device__ __forceinline__ void exact_groups(const int32_t *s, uint32_t *mag, uint32_t &sx) {
-    constexpr int NG = ExactShape<N, G>::NG;
+__device__ __forceinline__ void exact_term(const int32_t *s, uint32_t *acc, uint32_t odd) {
+    using S = ExactShape<N, G>;
+    constexpr int NG = S::NG, NL = S::NL;
+    // exact group products (|x| < 2^31 by the host's grouping); the sign is
+    // the XOR of the group signs and the Glynn sign
+    uint32_t sx = odd << 31;
+    uint32_t mag[NG];
 #pragma unroll
     for (int g = 0; g < NG; g++) {
         int32_t x = s[g * G];
@@ -118,47 +115,6 @@ __device__ __forceinline__ void exact_groups(const int32_t *s, uint32_t *mag, ui
             if (g * G + t < N) x *= s[g * G + t];
         sx ^= (uint32_t)x;
         mag[g] = (uint32_t)abs(x);
-    }
-}
-template <int N, int G>
-__device__ __forceinline__ void exact_groups(const float *s, uint32_t *mag, uint32_t &sx) {
-    // float rows: exact pair products (|pair| < 2^22) on the FP32 pipes,
-    // magnitudes extracted with one FADD + LOP3, group products by IMUL
-    constexpr int NG = ExactShape<N, G>::NG;
-#pragma unroll
-    for (int g = 0; g < NG; g++) {
-        uint32_t x = 1;
-#pragma unroll
-        for (int t = 0; t < G; t += 2) {
-            const int i = g * G + t;
-            if (i < N) {
-                const float p = (t + 1 < G && i + 1 < N) ? s[i] * s[i + 1] : s[i];
-                sx ^= __float_as_uint(p);
-                const uint32_t mg = exact_fmag(p);
-                x = t == 0 ? mg : x * mg;
-            }
-        }
-        mag[g] = x;
-    }
-}
-
-// One Glynn term at the current row sums: acc += (-1)^(odd + signs) * prod s.
-// With zskip, a warp whose 32 terms are all zero skips the word product.
-template <int N, int G, typename T>
-__device__ __forceinline__ void exact_term(const T *s, uint32_t *acc, uint32_t odd, bool zskip) {
-    using S = ExactShape<N, G>;
-    constexpr int NG = S::NG, NL = S::NL;
-    // exact group products (< 2^31 by the host's grouping); the sign is the
-    // XOR of the factor signs and the Glynn sign
-    uint32_t sx = odd << 31;
-    uint32_t mag[NG];
-    exact_groups<N, G>(s, mag, sx);
-    if (zskip) {
-        bool nz = true;
-#pragma unroll
-        for (int g = 0; g < NG; g++) nz = nz && mag[g] != 0;
-        // vote among the lanes walking this step (ranges may end unevenly)
-        if (!__any_sync(__activemask(), nz)) return;
     }
     uint32_t P[NG];
     P[0] = mag[0];
@@ -178,19 +134,13 @@ __device__ __forceinline__ void exact_term(const T *s, uint32_t *acc, uint32_t o
 #endif
 }
 
-template <typename T> struct Vec4;
-template <> struct Vec4<int32_t> { using type = int4; };
-template <> struct Vec4<float> { using type = float4; };
-
 // Walk chunks [c_begin, c_end) (row sums s already at state c_begin*2^log_len)
 // adding every term into acc.  Returns false if the abort word was seen.
-// All lanes of a warp must call this together when zskip is set.
-template <int N, int G, typename T>
-__device__ __forceinline__ bool exact_walk(const T *tab, T *s, uint32_t *acc,
+template <int N, int G>
+__device__ __forceinline__ bool exact_walk(const int32_t *tab, int32_t *s, uint32_t *acc,
                                            uint64_t c_begin, uint64_t c_end, int log_len,
-                                           volatile const int *abort_flag, bool zskip) {
+                                           volatile const int *abort_flag) {
     using S = ExactShape<N, G>;
-    using V4 = typename Vec4<T>::type;
     constexpr int NP = S::NP, LOGU = S::LOGU, U = 1 << LOGU;
     const uint32_t Q = (1u << log_len) >> LOGU;
     for (uint64_t c = c_begin; c < c_end; c++) {
@@ -217,10 +167,11 @@ __device__ __forceinline__ bool exact_walk(const T *tab, T *s, uint32_t *acc,
                     sub = ((c >> (jc + 1)) & 1) == 0;
                 }
                 if (step) {
-                    const V4 *col = reinterpret_cast<const V4 *>(tab + (2 * j + sub) * NP);
+                    const int4 *col =
+                        reinterpret_cast<const int4 *>(tab + (2 * j + sub) * NP);
 #pragma unroll
                     for (int v = 0; v < NP / 4; v++) {
-                        const V4 d = col[v];
+                        const int4 d = col[v];
                         if (4 * v + 0 < N) s[4 * v + 0] += d.x;
                         if (4 * v + 1 < N) s[4 * v + 1] += d.y;
                         if (4 * v + 2 < N) s[4 * v + 2] += d.z;
@@ -228,7 +179,7 @@ __device__ __forceinline__ bool exact_walk(const T *tab, T *s, uint32_t *acc,
                     }
                 }
                 // chunks start at even states, so (-1)^g = (-1)^r
-                exact_term<N, G, T>(s, acc, (uint32_t)(r & 1), zskip);
+                exact_term<N, G>(s, acc, (uint32_t)(r & 1));
             }
         }
     }
@@ -244,7 +195,6 @@ struct ExactArgs {
     uint64_t chunks;           // chunks to walk: [chunk0, chunk0 + chunks)
     int log_len;               // >= LOGU, <= 30
     uint64_t chunk0;           // first chunk (0 for a whole traversal)
-    int zskip;                 // skip all-zero warp steps (0/1 matrices)
 };
 
 // Resident blocks per SM requested from ptxas: a register budget of about
@@ -257,16 +207,13 @@ __host__ __device__ constexpr int exact_min_blocks(int N) {
            : (65536 / (256 * (N + 64)));
 }
 
-// FP: row sums kept as float (the host selects it when every row bound is
-// < 2^11, so row sums, pair products and the 2^23 magnitude trick are exact).
-template <int N, int G, bool FP>
+template <int N, int G>
 __global__ void __launch_bounds__(256, exact_min_blocks(N))
 exact_glynn_kernel(ExactArgs a) {
     using S = ExactShape<N, G>;
-    using T = typename std::conditional<FP, float, int32_t>::type;
     constexpr int NP = S::NP, NL = S::NL, NCOL = N - 1;
     extern __shared__ int4 esmem[];
-    T *tab = reinterpret_cast<T *>(esmem);
+    int32_t *tab = reinterpret_cast<int32_t *>(esmem);
     for (int i = threadIdx.x; i < NCOL * 2 * NP / 4; i += blockDim.x)
         esmem[i] = reinterpret_cast<const int4 *>(a.tab)[i];
     __syncthreads();
@@ -276,16 +223,15 @@ exact_glynn_kernel(ExactArgs a) {
     for (int l = 0; l < NL; l++) acc[l] = 0;
 
     // one contiguous, balanced range of chunks per thread
-    const uint64_t nthr = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t T = (uint64_t)gridDim.x * blockDim.x;
     const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const uint64_t c_begin = a.chunk0 + tid * a.chunks / nthr;
-    const uint64_t c_end = a.chunk0 + (tid + 1) * a.chunks / nthr;
+    const uint64_t c_begin = a.chunk0 + tid * a.chunks / T;
+    const uint64_t c_end = a.chunk0 + (tid + 1) * a.chunks / T;
     bool aborted = false;
     if (c_begin < c_end) {
-        T s[N];
-        exact_init<N, T>(tab, reinterpret_cast<const T *>(a.init), s, c_begin << a.log_len);
-        aborted = !exact_walk<N, G, T>(tab, s, acc, c_begin, c_end, a.log_len, a.abort_flag,
-                                       a.zskip != 0);
+        int32_t s[N];
+        exact_init<N>(tab, a.init, s, c_begin << a.log_len);
+        aborted = !exact_walk<N, G>(tab, s, acc, c_begin, c_end, a.log_len, a.abort_flag);
     }
 
     // Block reduction: word l < NL-1 contributes acc[l] (unsigned), the top
@@ -312,39 +258,39 @@ exact_glynn_kernel(ExactArgs a) {
     if (threadIdx.x == 0 && any_abort) atomicExch(a.status, 1);
 }
 
-template <int N, int G, bool FP>
+template <int N, int G>
 cudaError_t launch_exact_glynn(const ExactArgs &args, int blocks,
                                cudaStream_t stream) {
     constexpr int NP = ExactShape<N, G>::NP;
     const size_t smem = (size_t)(N - 1) * 2 * NP * sizeof(int32_t);
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(
-            exact_glynn_kernel<N, G, FP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            exact_glynn_kernel<N, G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
             (int)smem);
         if (e != cudaSuccess) return e;
     }
-    exact_glynn_kernel<N, G, FP><<<blocks, 256, smem, stream>>>(args);
+    exact_glynn_kernel<N, G><<<blocks, 256, smem, stream>>>(args);
     return cudaGetLastError();
 }
 
-template <int N, int G, bool FP>
+template <int N, int G>
 int occupancy_exact_glynn() {
     constexpr int NP = ExactShape<N, G>::NP;
     const size_t smem = (size_t)(N - 1) * 2 * NP * sizeof(int32_t);
     if (smem > 48 * 1024)
-        cudaFuncSetAttribute(exact_glynn_kernel<N, G, FP>,
+        cudaFuncSetAttribute(exact_glynn_kernel<N, G>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, exact_glynn_kernel<N, G, FP>,
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, exact_glynn_kernel<N, G>,
                                                       256, smem) != cudaSuccess)
         return 1;
     return nb < 1 ? 1 : nb;
 }
 
-// Compiled (N, G, FP) shapes; returns cudaErrorInvalidValue / 0 when absent.
-cudaError_t launch_exact_any(int N, int G, bool fp, const ExactArgs &args, int blocks,
+// Compiled (N, G) pairs; returns cudaErrorInvalidValue / 0 when absent.
+cudaError_t launch_exact_any(int N, int G, const ExactArgs &args, int blocks,
                              cudaStream_t stream);
-int occupancy_exact_any(int N, int G, bool fp);
-bool exact_compiled(int N, int G, bool fp);
+int occupancy_exact_any(int N, int G);
+bool exact_compiled(int N, int G);
 
 }  // namespace pg

@@ -1,122 +1,106 @@
-// Instantiations of the exact Glynn kernel (part 1 of 12).
+// Instantiations of the exact Glynn kernel (part 1 of 8).
 #include "exact_glynn.cuh"
 
 namespace pg {
 
-bool exact_dispatch_1(int key, const ExactArgs *args, int blocks,
+bool exact_dispatch_1(int N, int G, const ExactArgs *args, int blocks,
                        cudaStream_t stream, cudaError_t *err, int *occ) {
-    switch (key) {
-    case 36:
-        if (args) *err = launch_exact_glynn<2, 2, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<2, 2, false>();
+    switch (N * 8 + G) {
+    case 18:
+        if (args) *err = launch_exact_glynn<2, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<2, 2>();
         return true;
-    case 86:
-        if (args) *err = launch_exact_glynn<5, 3, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<5, 3, false>();
+    case 41:
+        if (args) *err = launch_exact_glynn<5, 1>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<5, 1>();
         return true;
-    case 118:
-        if (args) *err = launch_exact_glynn<7, 3, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<7, 3, false>();
+    case 57:
+        if (args) *err = launch_exact_glynn<7, 1>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<7, 1>();
         return true;
-    case 150:
-        if (args) *err = launch_exact_glynn<9, 3, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<9, 3, false>();
+    case 73:
+        if (args) *err = launch_exact_glynn<9, 1>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<9, 1>();
         return true;
-    case 182:
-        if (args) *err = launch_exact_glynn<11, 3, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<11, 3, false>();
+    case 89:
+        if (args) *err = launch_exact_glynn<11, 1>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<11, 1>();
         return true;
-    case 214:
-        if (args) *err = launch_exact_glynn<13, 3, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<13, 3, false>();
+    case 105:
+        if (args) *err = launch_exact_glynn<13, 1>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<13, 1>();
         return true;
-    case 246:
-        if (args) *err = launch_exact_glynn<15, 3, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<15, 3, false>();
+    case 121:
+        if (args) *err = launch_exact_glynn<15, 1>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<15, 1>();
         return true;
-    case 280:
-        if (args) *err = launch_exact_glynn<17, 4, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<17, 4, false>();
+    case 138:
+        if (args) *err = launch_exact_glynn<17, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<17, 2>();
         return true;
-    case 313:
-        if (args) *err = launch_exact_glynn<19, 4, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<19, 4, true>();
+    case 156:
+        if (args) *err = launch_exact_glynn<19, 4>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<19, 4>();
         return true;
-    case 358:
-        if (args) *err = launch_exact_glynn<22, 3, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<22, 3, false>();
+    case 179:
+        if (args) *err = launch_exact_glynn<22, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<22, 3>();
         return true;
-    case 394:
-        if (args) *err = launch_exact_glynn<24, 5, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<24, 5, false>();
+    case 197:
+        if (args) *err = launch_exact_glynn<24, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<24, 5>();
         return true;
-    case 409:
-        if (args) *err = launch_exact_glynn<25, 4, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<25, 4, true>();
+    case 211:
+        if (args) *err = launch_exact_glynn<26, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<26, 3>();
         return true;
-    case 436:
-        if (args) *err = launch_exact_glynn<27, 2, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<27, 2, false>();
+    case 222:
+        if (args) *err = launch_exact_glynn<27, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<27, 6>();
         return true;
-    case 458:
-        if (args) *err = launch_exact_glynn<28, 5, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<28, 5, false>();
+    case 236:
+        if (args) *err = launch_exact_glynn<29, 4>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<29, 4>();
         return true;
-    case 473:
-        if (args) *err = launch_exact_glynn<29, 4, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<29, 4, true>();
+    case 250:
+        if (args) *err = launch_exact_glynn<31, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<31, 2>();
         return true;
-    case 500:
-        if (args) *err = launch_exact_glynn<31, 2, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<31, 2, false>();
+    case 261:
+        if (args) *err = launch_exact_glynn<32, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<32, 5>();
         return true;
-    case 522:
-        if (args) *err = launch_exact_glynn<32, 5, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<32, 5, false>();
+    case 277:
+        if (args) *err = launch_exact_glynn<34, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<34, 5>();
         return true;
-    case 539:
-        if (args) *err = launch_exact_glynn<33, 5, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<33, 5, true>();
+    case 293:
+        if (args) *err = launch_exact_glynn<36, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<36, 5>();
         return true;
-    case 570:
-        if (args) *err = launch_exact_glynn<35, 5, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<35, 5, false>();
+    case 309:
+        if (args) *err = launch_exact_glynn<38, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<38, 5>();
         return true;
-    case 587:
-        if (args) *err = launch_exact_glynn<36, 5, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<36, 5, true>();
+    case 325:
+        if (args) *err = launch_exact_glynn<40, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<40, 5>();
         return true;
-    case 618:
-        if (args) *err = launch_exact_glynn<38, 5, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<38, 5, false>();
+    case 341:
+        if (args) *err = launch_exact_glynn<42, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<42, 5>();
         return true;
-    case 635:
-        if (args) *err = launch_exact_glynn<39, 5, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<39, 5, true>();
+    case 357:
+        if (args) *err = launch_exact_glynn<44, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<44, 5>();
         return true;
-    case 666:
-        if (args) *err = launch_exact_glynn<41, 5, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<41, 5, false>();
+    case 373:
+        if (args) *err = launch_exact_glynn<46, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<46, 5>();
         return true;
-    case 683:
-        if (args) *err = launch_exact_glynn<42, 5, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<42, 5, true>();
-        return true;
-    case 714:
-        if (args) *err = launch_exact_glynn<44, 5, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<44, 5, false>();
-        return true;
-    case 731:
-        if (args) *err = launch_exact_glynn<45, 5, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<45, 5, true>();
-        return true;
-    case 762:
-        if (args) *err = launch_exact_glynn<47, 5, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<47, 5, false>();
-        return true;
-    case 779:
-        if (args) *err = launch_exact_glynn<48, 5, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<48, 5, true>();
+    case 389:
+        if (args) *err = launch_exact_glynn<48, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<48, 5>();
         return true;
     default: return false;
     }

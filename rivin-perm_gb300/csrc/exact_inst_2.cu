@@ -1,122 +1,106 @@
-// Instantiations of the exact Glynn kernel (part 2 of 12).
+// Instantiations of the exact Glynn kernel (part 2 of 8).
 #include "exact_glynn.cuh"
 
 namespace pg {
 
-bool exact_dispatch_2(int key, const ExactArgs *args, int blocks,
+bool exact_dispatch_2(int N, int G, const ExactArgs *args, int blocks,
                        cudaStream_t stream, cudaError_t *err, int *occ) {
-    switch (key) {
-    case 50:
-        if (args) *err = launch_exact_glynn<3, 1, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<3, 1, false>();
+    switch (N * 8 + G) {
+    case 25:
+        if (args) *err = launch_exact_glynn<3, 1>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<3, 1>();
         return true;
-    case 88:
-        if (args) *err = launch_exact_glynn<5, 4, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<5, 4, false>();
+    case 42:
+        if (args) *err = launch_exact_glynn<5, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<5, 2>();
         return true;
-    case 120:
-        if (args) *err = launch_exact_glynn<7, 4, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<7, 4, false>();
+    case 58:
+        if (args) *err = launch_exact_glynn<7, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<7, 2>();
         return true;
-    case 152:
-        if (args) *err = launch_exact_glynn<9, 4, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<9, 4, false>();
+    case 74:
+        if (args) *err = launch_exact_glynn<9, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<9, 2>();
         return true;
-    case 184:
-        if (args) *err = launch_exact_glynn<11, 4, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<11, 4, false>();
+    case 90:
+        if (args) *err = launch_exact_glynn<11, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<11, 2>();
         return true;
-    case 216:
-        if (args) *err = launch_exact_glynn<13, 4, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<13, 4, false>();
+    case 106:
+        if (args) *err = launch_exact_glynn<13, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<13, 2>();
         return true;
-    case 248:
-        if (args) *err = launch_exact_glynn<15, 4, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<15, 4, false>();
+    case 122:
+        if (args) *err = launch_exact_glynn<15, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<15, 2>();
         return true;
-    case 279:
-        if (args) *err = launch_exact_glynn<17, 3, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<17, 3, true>();
+    case 139:
+        if (args) *err = launch_exact_glynn<17, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<17, 3>();
         return true;
-    case 324:
-        if (args) *err = launch_exact_glynn<20, 2, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<20, 2, false>();
+    case 162:
+        if (args) *err = launch_exact_glynn<20, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<20, 2>();
         return true;
-    case 360:
-        if (args) *err = launch_exact_glynn<22, 4, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<22, 4, false>();
+    case 180:
+        if (args) *err = launch_exact_glynn<22, 4>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<22, 4>();
         return true;
-    case 396:
-        if (args) *err = launch_exact_glynn<24, 6, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<24, 6, false>();
+    case 198:
+        if (args) *err = launch_exact_glynn<24, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<24, 6>();
         return true;
-    case 411:
-        if (args) *err = launch_exact_glynn<25, 5, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<25, 5, true>();
+    case 212:
+        if (args) *err = launch_exact_glynn<26, 4>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<26, 4>();
         return true;
-    case 438:
-        if (args) *err = launch_exact_glynn<27, 3, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<27, 3, false>();
+    case 226:
+        if (args) *err = launch_exact_glynn<28, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<28, 2>();
         return true;
-    case 460:
-        if (args) *err = launch_exact_glynn<28, 6, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<28, 6, false>();
+    case 237:
+        if (args) *err = launch_exact_glynn<29, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<29, 5>();
         return true;
-    case 475:
-        if (args) *err = launch_exact_glynn<29, 5, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<29, 5, true>();
+    case 251:
+        if (args) *err = launch_exact_glynn<31, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<31, 3>();
         return true;
-    case 502:
-        if (args) *err = launch_exact_glynn<31, 3, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<31, 3, false>();
+    case 262:
+        if (args) *err = launch_exact_glynn<32, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<32, 6>();
         return true;
-    case 524:
-        if (args) *err = launch_exact_glynn<32, 6, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<32, 6, false>();
+    case 278:
+        if (args) *err = launch_exact_glynn<34, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<34, 6>();
         return true;
-    case 541:
-        if (args) *err = launch_exact_glynn<33, 6, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<33, 6, true>();
+    case 294:
+        if (args) *err = launch_exact_glynn<36, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<36, 6>();
         return true;
-    case 572:
-        if (args) *err = launch_exact_glynn<35, 6, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<35, 6, false>();
+    case 310:
+        if (args) *err = launch_exact_glynn<38, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<38, 6>();
         return true;
-    case 589:
-        if (args) *err = launch_exact_glynn<36, 6, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<36, 6, true>();
+    case 326:
+        if (args) *err = launch_exact_glynn<40, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<40, 6>();
         return true;
-    case 620:
-        if (args) *err = launch_exact_glynn<38, 6, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<38, 6, false>();
+    case 342:
+        if (args) *err = launch_exact_glynn<42, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<42, 6>();
         return true;
-    case 637:
-        if (args) *err = launch_exact_glynn<39, 6, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<39, 6, true>();
+    case 358:
+        if (args) *err = launch_exact_glynn<44, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<44, 6>();
         return true;
-    case 668:
-        if (args) *err = launch_exact_glynn<41, 6, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<41, 6, false>();
+    case 374:
+        if (args) *err = launch_exact_glynn<46, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<46, 6>();
         return true;
-    case 685:
-        if (args) *err = launch_exact_glynn<42, 6, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<42, 6, true>();
-        return true;
-    case 716:
-        if (args) *err = launch_exact_glynn<44, 6, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<44, 6, false>();
-        return true;
-    case 733:
-        if (args) *err = launch_exact_glynn<45, 6, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<45, 6, true>();
-        return true;
-    case 764:
-        if (args) *err = launch_exact_glynn<47, 6, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<47, 6, false>();
-        return true;
-    case 781:
-        if (args) *err = launch_exact_glynn<48, 6, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<48, 6, true>();
+    case 390:
+        if (args) *err = launch_exact_glynn<48, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<48, 6>();
         return true;
     default: return false;
     }

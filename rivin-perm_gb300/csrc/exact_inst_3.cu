@@ -1,118 +1,102 @@
-// Instantiations of the exact Glynn kernel (part 3 of 12).
+// Instantiations of the exact Glynn kernel (part 3 of 8).
 #include "exact_glynn.cuh"
 
 namespace pg {
 
-bool exact_dispatch_3(int key, const ExactArgs *args, int blocks,
+bool exact_dispatch_3(int N, int G, const ExactArgs *args, int blocks,
                        cudaStream_t stream, cudaError_t *err, int *occ) {
-    switch (key) {
-    case 52:
-        if (args) *err = launch_exact_glynn<3, 2, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<3, 2, false>();
+    switch (N * 8 + G) {
+    case 26:
+        if (args) *err = launch_exact_glynn<3, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<3, 2>();
         return true;
-    case 87:
-        if (args) *err = launch_exact_glynn<5, 3, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<5, 3, true>();
+    case 43:
+        if (args) *err = launch_exact_glynn<5, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<5, 3>();
         return true;
-    case 119:
-        if (args) *err = launch_exact_glynn<7, 3, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<7, 3, true>();
+    case 59:
+        if (args) *err = launch_exact_glynn<7, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<7, 3>();
         return true;
-    case 151:
-        if (args) *err = launch_exact_glynn<9, 3, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<9, 3, true>();
+    case 75:
+        if (args) *err = launch_exact_glynn<9, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<9, 3>();
         return true;
-    case 183:
-        if (args) *err = launch_exact_glynn<11, 3, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<11, 3, true>();
+    case 91:
+        if (args) *err = launch_exact_glynn<11, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<11, 3>();
         return true;
-    case 215:
-        if (args) *err = launch_exact_glynn<13, 3, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<13, 3, true>();
+    case 107:
+        if (args) *err = launch_exact_glynn<13, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<13, 3>();
         return true;
-    case 247:
-        if (args) *err = launch_exact_glynn<15, 3, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<15, 3, true>();
+    case 123:
+        if (args) *err = launch_exact_glynn<15, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<15, 3>();
         return true;
-    case 281:
-        if (args) *err = launch_exact_glynn<17, 4, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<17, 4, true>();
+    case 140:
+        if (args) *err = launch_exact_glynn<17, 4>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<17, 4>();
         return true;
-    case 326:
-        if (args) *err = launch_exact_glynn<20, 3, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<20, 3, false>();
+    case 163:
+        if (args) *err = launch_exact_glynn<20, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<20, 3>();
         return true;
-    case 359:
-        if (args) *err = launch_exact_glynn<22, 3, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<22, 3, true>();
+    case 186:
+        if (args) *err = launch_exact_glynn<23, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<23, 2>();
         return true;
-    case 391:
-        if (args) *err = launch_exact_glynn<24, 3, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<24, 3, true>();
+    case 202:
+        if (args) *err = launch_exact_glynn<25, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<25, 2>();
         return true;
-    case 413:
-        if (args) *err = launch_exact_glynn<25, 6, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<25, 6, true>();
+    case 213:
+        if (args) *err = launch_exact_glynn<26, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<26, 5>();
         return true;
-    case 440:
-        if (args) *err = launch_exact_glynn<27, 4, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<27, 4, false>();
+    case 227:
+        if (args) *err = launch_exact_glynn<28, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<28, 3>();
         return true;
-    case 455:
-        if (args) *err = launch_exact_glynn<28, 3, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<28, 3, true>();
+    case 238:
+        if (args) *err = launch_exact_glynn<29, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<29, 6>();
         return true;
-    case 477:
-        if (args) *err = launch_exact_glynn<29, 6, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<29, 6, true>();
+    case 252:
+        if (args) *err = launch_exact_glynn<31, 4>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<31, 4>();
         return true;
-    case 504:
-        if (args) *err = launch_exact_glynn<31, 4, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<31, 4, false>();
+    case 267:
+        if (args) *err = launch_exact_glynn<33, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<33, 3>();
         return true;
-    case 519:
-        if (args) *err = launch_exact_glynn<32, 3, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<32, 3, true>();
+    case 283:
+        if (args) *err = launch_exact_glynn<35, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<35, 3>();
         return true;
-    case 550:
-        if (args) *err = launch_exact_glynn<34, 3, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<34, 3, false>();
+    case 299:
+        if (args) *err = launch_exact_glynn<37, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<37, 3>();
         return true;
-    case 567:
-        if (args) *err = launch_exact_glynn<35, 3, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<35, 3, true>();
+    case 315:
+        if (args) *err = launch_exact_glynn<39, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<39, 3>();
         return true;
-    case 598:
-        if (args) *err = launch_exact_glynn<37, 3, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<37, 3, false>();
+    case 331:
+        if (args) *err = launch_exact_glynn<41, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<41, 3>();
         return true;
-    case 615:
-        if (args) *err = launch_exact_glynn<38, 3, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<38, 3, true>();
+    case 347:
+        if (args) *err = launch_exact_glynn<43, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<43, 3>();
         return true;
-    case 646:
-        if (args) *err = launch_exact_glynn<40, 3, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<40, 3, false>();
+    case 363:
+        if (args) *err = launch_exact_glynn<45, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<45, 3>();
         return true;
-    case 663:
-        if (args) *err = launch_exact_glynn<41, 3, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<41, 3, true>();
-        return true;
-    case 694:
-        if (args) *err = launch_exact_glynn<43, 3, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<43, 3, false>();
-        return true;
-    case 711:
-        if (args) *err = launch_exact_glynn<44, 3, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<44, 3, true>();
-        return true;
-    case 742:
-        if (args) *err = launch_exact_glynn<46, 3, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<46, 3, false>();
-        return true;
-    case 759:
-        if (args) *err = launch_exact_glynn<47, 3, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<47, 3, true>();
+    case 379:
+        if (args) *err = launch_exact_glynn<47, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<47, 3>();
         return true;
     default: return false;
     }

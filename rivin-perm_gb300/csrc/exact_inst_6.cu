@@ -1,118 +1,102 @@
-// Instantiations of the exact Glynn kernel (part 6 of 12).
+// Instantiations of the exact Glynn kernel (part 6 of 8).
 #include "exact_glynn.cuh"
 
 namespace pg {
 
-bool exact_dispatch_6(int key, const ExactArgs *args, int blocks,
+bool exact_dispatch_6(int N, int G, const ExactArgs *args, int blocks,
                        cudaStream_t stream, cudaError_t *err, int *occ) {
-    switch (key) {
-    case 68:
-        if (args) *err = launch_exact_glynn<4, 2, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<4, 2, false>();
+    switch (N * 8 + G) {
+    case 34:
+        if (args) *err = launch_exact_glynn<4, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<4, 2>();
         return true;
-    case 100:
-        if (args) *err = launch_exact_glynn<6, 2, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<6, 2, false>();
+    case 50:
+        if (args) *err = launch_exact_glynn<6, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<6, 2>();
         return true;
-    case 132:
-        if (args) *err = launch_exact_glynn<8, 2, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<8, 2, false>();
+    case 66:
+        if (args) *err = launch_exact_glynn<8, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<8, 2>();
         return true;
-    case 164:
-        if (args) *err = launch_exact_glynn<10, 2, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<10, 2, false>();
+    case 82:
+        if (args) *err = launch_exact_glynn<10, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<10, 2>();
         return true;
-    case 196:
-        if (args) *err = launch_exact_glynn<12, 2, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<12, 2, false>();
+    case 98:
+        if (args) *err = launch_exact_glynn<12, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<12, 2>();
         return true;
-    case 228:
-        if (args) *err = launch_exact_glynn<14, 2, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<14, 2, false>();
+    case 114:
+        if (args) *err = launch_exact_glynn<14, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<14, 2>();
         return true;
-    case 260:
-        if (args) *err = launch_exact_glynn<16, 2, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<16, 2, false>();
+    case 130:
+        if (args) *err = launch_exact_glynn<16, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<16, 2>();
         return true;
-    case 296:
-        if (args) *err = launch_exact_glynn<18, 4, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<18, 4, false>();
+    case 148:
+        if (args) *err = launch_exact_glynn<18, 4>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<18, 4>();
         return true;
-    case 329:
-        if (args) *err = launch_exact_glynn<20, 4, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<20, 4, true>();
+    case 171:
+        if (args) *err = launch_exact_glynn<21, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<21, 3>();
         return true;
-    case 374:
-        if (args) *err = launch_exact_glynn<23, 3, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<23, 3, false>();
+    case 194:
+        if (args) *err = launch_exact_glynn<24, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<24, 2>();
         return true;
-    case 397:
-        if (args) *err = launch_exact_glynn<24, 6, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<24, 6, true>();
+    case 205:
+        if (args) *err = launch_exact_glynn<25, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<25, 5>();
         return true;
-    case 424:
-        if (args) *err = launch_exact_glynn<26, 4, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<26, 4, false>();
+    case 219:
+        if (args) *err = launch_exact_glynn<27, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<27, 3>();
         return true;
-    case 439:
-        if (args) *err = launch_exact_glynn<27, 3, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<27, 3, true>();
+    case 230:
+        if (args) *err = launch_exact_glynn<28, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<28, 6>();
         return true;
-    case 461:
-        if (args) *err = launch_exact_glynn<28, 6, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<28, 6, true>();
+    case 244:
+        if (args) *err = launch_exact_glynn<30, 4>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<30, 4>();
         return true;
-    case 488:
-        if (args) *err = launch_exact_glynn<30, 4, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<30, 4, false>();
+    case 258:
+        if (args) *err = launch_exact_glynn<32, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<32, 2>();
         return true;
-    case 503:
-        if (args) *err = launch_exact_glynn<31, 3, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<31, 3, true>();
+    case 270:
+        if (args) *err = launch_exact_glynn<33, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<33, 6>();
         return true;
-    case 525:
-        if (args) *err = launch_exact_glynn<32, 6, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<32, 6, true>();
+    case 286:
+        if (args) *err = launch_exact_glynn<35, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<35, 6>();
         return true;
-    case 556:
-        if (args) *err = launch_exact_glynn<34, 6, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<34, 6, false>();
+    case 302:
+        if (args) *err = launch_exact_glynn<37, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<37, 6>();
         return true;
-    case 573:
-        if (args) *err = launch_exact_glynn<35, 6, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<35, 6, true>();
+    case 318:
+        if (args) *err = launch_exact_glynn<39, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<39, 6>();
         return true;
-    case 604:
-        if (args) *err = launch_exact_glynn<37, 6, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<37, 6, false>();
+    case 334:
+        if (args) *err = launch_exact_glynn<41, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<41, 6>();
         return true;
-    case 621:
-        if (args) *err = launch_exact_glynn<38, 6, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<38, 6, true>();
+    case 350:
+        if (args) *err = launch_exact_glynn<43, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<43, 6>();
         return true;
-    case 652:
-        if (args) *err = launch_exact_glynn<40, 6, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<40, 6, false>();
+    case 366:
+        if (args) *err = launch_exact_glynn<45, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<45, 6>();
         return true;
-    case 669:
-        if (args) *err = launch_exact_glynn<41, 6, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<41, 6, true>();
-        return true;
-    case 700:
-        if (args) *err = launch_exact_glynn<43, 6, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<43, 6, false>();
-        return true;
-    case 717:
-        if (args) *err = launch_exact_glynn<44, 6, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<44, 6, true>();
-        return true;
-    case 748:
-        if (args) *err = launch_exact_glynn<46, 6, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<46, 6, false>();
-        return true;
-    case 765:
-        if (args) *err = launch_exact_glynn<47, 6, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<47, 6, true>();
+    case 382:
+        if (args) *err = launch_exact_glynn<47, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<47, 6>();
         return true;
     default: return false;
     }

@@ -1,118 +1,102 @@
-// Instantiations of the exact Glynn kernel (part 7 of 12).
+// Instantiations of the exact Glynn kernel (part 7 of 8).
 #include "exact_glynn.cuh"
 
 namespace pg {
 
-bool exact_dispatch_7(int key, const ExactArgs *args, int blocks,
+bool exact_dispatch_7(int N, int G, const ExactArgs *args, int blocks,
                        cudaStream_t stream, cudaError_t *err, int *occ) {
-    switch (key) {
-    case 70:
-        if (args) *err = launch_exact_glynn<4, 3, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<4, 3, false>();
+    switch (N * 8 + G) {
+    case 35:
+        if (args) *err = launch_exact_glynn<4, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<4, 3>();
         return true;
-    case 102:
-        if (args) *err = launch_exact_glynn<6, 3, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<6, 3, false>();
+    case 51:
+        if (args) *err = launch_exact_glynn<6, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<6, 3>();
         return true;
-    case 134:
-        if (args) *err = launch_exact_glynn<8, 3, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<8, 3, false>();
+    case 67:
+        if (args) *err = launch_exact_glynn<8, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<8, 3>();
         return true;
-    case 166:
-        if (args) *err = launch_exact_glynn<10, 3, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<10, 3, false>();
+    case 83:
+        if (args) *err = launch_exact_glynn<10, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<10, 3>();
         return true;
-    case 198:
-        if (args) *err = launch_exact_glynn<12, 3, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<12, 3, false>();
+    case 99:
+        if (args) *err = launch_exact_glynn<12, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<12, 3>();
         return true;
-    case 230:
-        if (args) *err = launch_exact_glynn<14, 3, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<14, 3, false>();
+    case 115:
+        if (args) *err = launch_exact_glynn<14, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<14, 3>();
         return true;
-    case 262:
-        if (args) *err = launch_exact_glynn<16, 3, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<16, 3, false>();
+    case 131:
+        if (args) *err = launch_exact_glynn<16, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<16, 3>();
         return true;
-    case 295:
-        if (args) *err = launch_exact_glynn<18, 3, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<18, 3, true>();
+    case 154:
+        if (args) *err = launch_exact_glynn<19, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<19, 2>();
         return true;
-    case 340:
-        if (args) *err = launch_exact_glynn<21, 2, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<21, 2, false>();
+    case 172:
+        if (args) *err = launch_exact_glynn<21, 4>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<21, 4>();
         return true;
-    case 376:
-        if (args) *err = launch_exact_glynn<23, 4, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<23, 4, false>();
+    case 195:
+        if (args) *err = launch_exact_glynn<24, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<24, 3>();
         return true;
-    case 404:
-        if (args) *err = launch_exact_glynn<25, 2, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<25, 2, false>();
+    case 206:
+        if (args) *err = launch_exact_glynn<25, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<25, 6>();
         return true;
-    case 426:
-        if (args) *err = launch_exact_glynn<26, 5, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<26, 5, false>();
+    case 220:
+        if (args) *err = launch_exact_glynn<27, 4>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<27, 4>();
         return true;
-    case 441:
-        if (args) *err = launch_exact_glynn<27, 4, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<27, 4, true>();
+    case 234:
+        if (args) *err = launch_exact_glynn<29, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<29, 2>();
         return true;
-    case 468:
-        if (args) *err = launch_exact_glynn<29, 2, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<29, 2, false>();
+    case 245:
+        if (args) *err = launch_exact_glynn<30, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<30, 5>();
         return true;
-    case 490:
-        if (args) *err = launch_exact_glynn<30, 5, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<30, 5, false>();
+    case 259:
+        if (args) *err = launch_exact_glynn<32, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<32, 3>();
         return true;
-    case 505:
-        if (args) *err = launch_exact_glynn<31, 4, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<31, 4, true>();
+    case 275:
+        if (args) *err = launch_exact_glynn<34, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<34, 3>();
         return true;
-    case 534:
-        if (args) *err = launch_exact_glynn<33, 3, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<33, 3, false>();
+    case 291:
+        if (args) *err = launch_exact_glynn<36, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<36, 3>();
         return true;
-    case 551:
-        if (args) *err = launch_exact_glynn<34, 3, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<34, 3, true>();
+    case 307:
+        if (args) *err = launch_exact_glynn<38, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<38, 3>();
         return true;
-    case 582:
-        if (args) *err = launch_exact_glynn<36, 3, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<36, 3, false>();
+    case 323:
+        if (args) *err = launch_exact_glynn<40, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<40, 3>();
         return true;
-    case 599:
-        if (args) *err = launch_exact_glynn<37, 3, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<37, 3, true>();
+    case 339:
+        if (args) *err = launch_exact_glynn<42, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<42, 3>();
         return true;
-    case 630:
-        if (args) *err = launch_exact_glynn<39, 3, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<39, 3, false>();
+    case 355:
+        if (args) *err = launch_exact_glynn<44, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<44, 3>();
         return true;
-    case 647:
-        if (args) *err = launch_exact_glynn<40, 3, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<40, 3, true>();
+    case 371:
+        if (args) *err = launch_exact_glynn<46, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<46, 3>();
         return true;
-    case 678:
-        if (args) *err = launch_exact_glynn<42, 3, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<42, 3, false>();
-        return true;
-    case 695:
-        if (args) *err = launch_exact_glynn<43, 3, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<43, 3, true>();
-        return true;
-    case 726:
-        if (args) *err = launch_exact_glynn<45, 3, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<45, 3, false>();
-        return true;
-    case 743:
-        if (args) *err = launch_exact_glynn<46, 3, true>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<46, 3, true>();
-        return true;
-    case 774:
-        if (args) *err = launch_exact_glynn<48, 3, false>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<48, 3, false>();
+    case 387:
+        if (args) *err = launch_exact_glynn<48, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<48, 3>();
         return true;
     default: return false;
     }

@@ -48,39 +48,22 @@ static bool group_rows(const std::vector<uint64_t> &B, int n, int G,
     return true;
 }
 
-// Picks the kernel shape: the largest compiled group size that admits a
-// grouping; float rows (fp) when every row bound is < 2^11 (row sums and
-// pair products then stay exact in FP32); zero-skip for 0/1 matrices, whose
-// Glynn terms are mostly zero (a row sum of an even-degree row vanishes
-// with probability ~ sqrt(2 / (pi * degree))).
-static int choose_group(const int64_t *A, int n, std::vector<int> *order,
-                        bool *fp = nullptr, bool *zskip = nullptr) {
+// Picks the largest compiled group size that admits a grouping.
+static int choose_group(const int64_t *A, int n, std::vector<int> *order) {
     if (n < 2 || n > 48) return 0;
     std::vector<uint64_t> B(n);
-    uint64_t maxB = 0;
-    bool binary = true;
     for (int i = 0; i < n; i++) {
         unsigned __int128 s = 0;
         for (int j = 0; j < n; j++) {
             const int64_t v = A[(size_t)i * n + j];
             s += v < 0 ? (unsigned __int128)(-(__int128)v) : (unsigned __int128)v;
-            binary = binary && (v == 0 || v == 1);
         }
         if (s >= ((unsigned __int128)1 << 30)) return 0;
         B[i] = (uint64_t)s;
-        if (B[i] > maxB) maxB = B[i];
     }
-    const bool want_fp = maxB < 2048;
-    for (int pass = want_fp ? 0 : 1; pass < 2; pass++) {
-        const bool f = pass == 0;
-        for (int G = 6; G >= 1; G--) {
-            if (!exact_compiled(n, G, f)) continue;
-            if (group_rows(B, n, G, order)) {
-                if (fp) *fp = f;
-                if (zskip) *zskip = binary;
-                return G;
-            }
-        }
+    for (int G = 6; G >= 1; G--) {
+        if (!exact_compiled(n, G)) continue;
+        if (group_rows(B, n, G, order)) return G;
     }
     return 0;
 }
@@ -114,7 +97,6 @@ static void add_i64_at(std::vector<uint32_t> &w, int pos, long long v) {
 // Everything one exact evaluation needs, built once on the host.
 struct ExactPlan {
     int n = 0, G = 0, NG = 0, NL = 0, need_bits = 0;
-    bool fp = false, zskip = false;
     ChunkPlan chunks{};
     uint64_t chunk0 = 0;
     uint64_t blocks = 0;
@@ -130,7 +112,7 @@ struct ExactPlan {
 
 static int plan_build(const int64_t *A, int n, ExactPlan *P) {
     std::vector<int> order;
-    const int G = choose_group(A, n, &order, &P->fp, &P->zskip);
+    const int G = choose_group(A, n, &order);
     if (!G) return fail(PG_EOVERFLOW, "row-sum bound exceeds the exact engine's fixed widths");
     DeviceInfo dev;
     int st = device_info(&dev);
@@ -150,27 +132,20 @@ static int plan_build(const int64_t *A, int n, ExactPlan *P) {
     P->image.assign(P->total, 0);
     int32_t *tab = (int32_t *)P->image.data();
     int32_t *init = (int32_t *)(P->image.data() + off_init);
-    float *ftab = (float *)tab, *finit = (float *)init;   // fp: same words as floats
     for (int ii = 0; ii < N; ii++) {
         const int64_t *row = A + (size_t)order[ii] * n;
         int64_t sum = 0;
         for (int j = 0; j < n; j++) sum += row[j];
-        if (P->fp) finit[ii] = (float)sum;
-        else init[ii] = (int32_t)sum;
+        init[ii] = (int32_t)sum;
         for (int j = 0; j < NCOL; j++) {
-            if (P->fp) {
-                ftab[(2 * j + 0) * NP + ii] = (float)(2 * row[j]);
-                ftab[(2 * j + 1) * NP + ii] = (float)(-2 * row[j]);
-            } else {
-                tab[(2 * j + 0) * NP + ii] = (int32_t)(2 * row[j]);
-                tab[(2 * j + 1) * NP + ii] = (int32_t)(-2 * row[j]);
-            }
+            tab[(2 * j + 0) * NP + ii] = (int32_t)(2 * row[j]);
+            tab[(2 * j + 1) * NP + ii] = (int32_t)(-2 * row[j]);
         }
     }
     // One resident wave of blocks (occupancy-limited), each thread owning a
     // contiguous range of ~128 chunks of >= 64 states; small orders use
     // fewer blocks so every thread still gets >= 512 states.
-    const int occ = occupancy_exact_any(N, G, P->fp);
+    const int occ = occupancy_exact_any(N, G);
     const int log_states = n - 1;
     uint64_t blocks = (uint64_t)occ * dev.sm_count;
     while (blocks > 1 && ((1ull << log_states) >> 9) < blocks * 256) blocks >>= 1;
@@ -206,9 +181,8 @@ static int plan_launch(ExactPlan *P, cudaStream_t stream) {
     args.chunks = P->chunks.chunks;
     args.log_len = P->chunks.log_len;
     args.chunk0 = P->chunk0;
-    args.zskip = P->zskip ? 1 : 0;
     PG_CUDA(cudaMemsetAsync(P->dev + P->off_acc, 0, P->total - P->off_acc, stream));
-    PG_CUDA(launch_exact_any(P->n, P->G, P->fp, args, (int)P->blocks, stream));
+    PG_CUDA(launch_exact_any(P->n, P->G, args, (int)P->blocks, stream));
     return PG_OK;
 }
 

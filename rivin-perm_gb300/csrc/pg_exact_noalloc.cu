@@ -86,7 +86,7 @@ extern "C" int pg_exact_permanent_noalloc(const int64_t *A, int n, uint32_t *out
         return fail(PG_ERANGE, "output limb count too small for the permanent bound");
     int order[48], G = 0;
     for (int g = 6; g >= 1 && !G; g--) {
-        if (!exact_compiled(n, g, false)) continue;
+        if (!exact_compiled(n, g)) continue;
         // greedy: largest bound into the group with the smallest log-product
         const int NG = (n + g - 1) / g;
         int cnt[48] = {0}, members[48][6];
@@ -162,7 +162,7 @@ extern "C" int pg_exact_permanent_noalloc(const int64_t *A, int n, uint32_t *out
     PG_CUDA(cudaMemsetAsync(scratch + off_acc, 0, total - off_acc, s));
 
     // launch shape as in the allocating path
-    const int occ = occupancy_exact_any(n, G, false);
+    const int occ = occupancy_exact_any(n, G);
     const int log_states = n - 1;
     uint64_t blocks = (uint64_t)occ * dev.sm_count;
     while (blocks > 1 && ((1ull << log_states) >> 9) < blocks * 256) blocks >>= 1;
@@ -183,8 +183,7 @@ extern "C" int pg_exact_permanent_noalloc(const int64_t *A, int n, uint32_t *out
     args.chunks = 1ull << (log_states - log_len);
     args.log_len = log_len;
     args.chunk0 = 0;
-    args.zskip = 0;
-    PG_CUDA(launch_exact_any(n, G, false, args, (int)blocks, s));
+    PG_CUDA(launch_exact_any(n, G, args, (int)blocks, s));
 
     long long acc[64];          // NL <= 18 for every compiled shape
     int status = 0;
