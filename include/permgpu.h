@@ -181,6 +181,17 @@ int pg_glynn_f64_dev(const double *A, int batch, int n, double *per,
                      void *stream);
 
 /*
+ * Complex FP64 Glynn permanent (forward) for a batch of complex matrices
+ * given as separate real and imaginary planes (device pointers, [batch][n]
+ * [n] each); per_re/per_im receive per(A_b), abs_sum (nullable) the error
+ * scale 2^(1-n) sum |terms|.  2 <= n <= 32.  Replaces
+ * permanent_parallel_complex (perm_parallel_cuda.cu:416-498).
+ */
+int pg_glynn_c64_dev(const double *Are, const double *Aim, int batch, int n,
+                     double *per_re, double *per_im, double *abs_sum,
+                     void *stream);
+
+/*
  * pg_exact_permanent for callers that cannot allocate memory (no
  * counterpart in the reference).  Code that runs during CUDA graph capture,
  * plug-ins whose host owns every device allocation, and services that must

@@ -67,6 +67,8 @@ def load():
         lib.or_glynn_range_mod_p.argtypes = [i64p, ctypes.c_int, ctypes.c_int64,
                                              ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int]
         lib.or_glynn_range_mod_p.restype = ctypes.c_int64
+        lib.or_glynn_c64.argtypes = [f64p, f64p, ctypes.c_int, f64p, f64p, f64p]
+        lib.or_glynn_c64.restype = None
         lib.or_max_threads.argtypes = []
         lib.or_max_threads.restype = ctypes.c_int
         _lib = lib
@@ -192,6 +194,18 @@ def glynn_f64(matrix, threads: int = 0):
     v = load().or_glynn_f64(a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), n,
                             int(threads or max_threads()), ctypes.byref(s))
     return float(v), float(s.value)
+
+
+def glynn_c64(matrix):
+    """(per, 2^(1-n) * sum |terms|) of a complex matrix, FP64 Kahan."""
+    a = np.asarray(matrix, dtype=np.complex128)
+    re = np.ascontiguousarray(a.real)
+    im = np.ascontiguousarray(a.imag)
+    n = a.shape[0] if a.ndim == 2 else 0
+    pr, pi, s = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    p = lambda x: x.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    load().or_glynn_c64(p(re), p(im), n, ctypes.byref(pr), ctypes.byref(pi), ctypes.byref(s))
+    return complex(pr.value, pi.value), s.value
 
 
 def glynn_f64_grad(matrix, threads: int = 0) -> np.ndarray:

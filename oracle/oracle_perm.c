@@ -356,6 +356,44 @@ double or_glynn_f64(const double *a, int n, int threads, double *abs_sum) {
     return ldexp(total, -(n - 1));
 }
 
+/* Complex Glynn in FP64 with a Kahan-compensated sum (serial):
+ * perm_parallel_cuda.cu:68-209 with IS_COMPLEX. */
+void or_glynn_c64(const double *are, const double *aim, int n, double *out_re,
+                  double *out_im, double *abs_sum) {
+    if (n <= 0) { *out_re = 1.0; *out_im = 0.0; if (abs_sum) *abs_sum = 1.0; return; }
+    if (n == 1) { *out_re = are[0]; *out_im = aim[0]; if (abs_sum) *abs_sum = hypot(are[0], aim[0]); return; }
+    double rr[64], ri[64];
+    for (int r = 0; r < n; r++) {
+        double sr = 0, si = 0;
+        for (int c = 0; c < n; c++) { sr += are[r * n + c]; si += aim[r * n + c]; }
+        rr[r] = sr; ri[r] = si;
+    }
+    double sr = 0, cr = 0, si = 0, ci = 0, as = 0;
+    int sign = 1;
+    uint64_t states = 1ULL << (n - 1);
+    for (uint64_t s = 0; s < states; s++) {
+        if (s) {
+            int c = __builtin_ctzll(s);
+            uint64_t gs = s ^ (s >> 1);
+            double f = ((gs >> c) & 1) ? -2.0 : 2.0;
+            for (int r = 0; r < n; r++) { rr[r] += f * are[r * n + c]; ri[r] += f * aim[r * n + c]; }
+            sign = -sign;
+        }
+        double pr = rr[0], pi = ri[0];
+        for (int r = 1; r < n; r++) {
+            double nr = pr * rr[r] - pi * ri[r];
+            pi = pr * ri[r] + pi * rr[r];
+            pr = nr;
+        }
+        double y = sign * pr - cr, t = sr + y; cr = (t - sr) - y; sr = t;
+        y = sign * pi - ci; t = si + y; ci = (t - si) - y; si = t;
+        as += hypot(pr, pi);
+    }
+    *out_re = ldexp(sr, -(n - 1));
+    *out_im = ldexp(si, -(n - 1));
+    if (abs_sum) *abs_sum = ldexp(as, -(n - 1));
+}
+
 /* Gradient by minors: grad[i*n+j] = per(A with row i and column j removed). */
 void or_glynn_f64_grad(const double *a, int n, int threads, double *grad) {
     if (n <= 0) return;

@@ -28,6 +28,11 @@
 
 #include "acc_chain.cuh"
 #include "mp_mul.cuh"
+#include "mp_mul_oop.cuh"
+
+#ifndef EXACT_MUL_OOP
+#define EXACT_MUL_OOP 0
+#endif
 
 #ifndef EXACT_LOGU
 #define EXACT_LOGU 2
@@ -53,7 +58,12 @@ __device__ __forceinline__ constexpr int exact_ctz_small(int r) {
 template <int G0, int NG>
 struct ProdChain {
     static __device__ __forceinline__ void run(uint32_t *P, const uint32_t *mag) {
-#if EXACT_MUL_PTX
+#if EXACT_MUL_OOP
+        uint32_t Q[G0 + 1];
+        MulWordOop<G0>::apply(P, Q, mag[G0]);
+#pragma unroll
+        for (int l = 0; l <= G0; l++) P[l] = Q[l];
+#elif EXACT_MUL_PTX
         MulWord<G0>::apply(P, mag[G0]);
 #else
         uint32_t carry = 0;

@@ -365,3 +365,191 @@ extern "C" int pg_glynn_f64_dev(const double *A, int batch, int n, double *per, 
     if (hstatus) return fail(PG_EABORT, "FP64 launch aborted by pg_abort()");
     return PG_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Complex FP64 Glynn permanent (forward), double-float complex arithmetic.
+// Same walk as glynn_f64_kernel (lane = row, shuffle butterfly for the row
+// product, exact FP64 re-initialisation every 2^log_block states, Kahan FP64
+// flushes into per-warp slots); complex counterpart of rivin-perm
+// permanent_glynn_kernel<true> (perm_parallel_cuda.cu:68-209).
+namespace pg {
+
+struct dc { df re, im; };
+
+__device__ __forceinline__ dc dc_mul(dc a, dc b) {
+    dc r;
+    r.re = df_add(df_mul(a.re, b.re), df_neg(df_mul(a.im, b.im)));
+    r.im = df_add(df_mul(a.re, b.im), df_mul(a.im, b.re));
+    return r;
+}
+
+struct C64Args {
+    const double *Are, *Aim;   // [batch][n][n]
+    int batch, log_w, log_block;
+    double *slots;             // [batch << log_w][8]: re sum/comp, im sum/comp, abs
+    volatile const int *abort_flag;
+    int *status;
+};
+
+template <int N>
+__global__ void __launch_bounds__(128) glynn_c64_kernel(C64Args a) {
+    constexpr int LEV = N <= 2 ? 1 : N <= 4 ? 2 : N <= 8 ? 3 : N <= 16 ? 4 : 5;
+    __shared__ dc tab[4][N - 1][32];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const long gw = (long)blockIdx.x * 4 + wib;
+    if (gw >= ((long)a.batch << a.log_w)) return;
+    const int b = (int)(gw >> a.log_w);
+    const uint64_t part = (uint64_t)(gw & ((1 << a.log_w) - 1));
+    const uint64_t per_warp = (1ull << (N - 1)) >> a.log_w;
+    const uint64_t g_begin = part * per_warp, g_end = g_begin + per_warp;
+    const double *Ar = a.Are + (size_t)b * N * N, *Ai = a.Aim + (size_t)b * N * N;
+    const bool live = lane < N;
+    // power-of-two row scaling by the row's sum of |re| + |im|
+    double rowsum = 0.0;
+    if (live)
+        for (int j = 0; j < N; j++) rowsum += fabs(Ar[lane * N + j]) + fabs(Ai[lane * N + j]);
+    int ex = 0;
+    if (live && rowsum > 0.0) { frexp(rowsum, &ex); ex = -ex; }
+    const double rs = ldexp(1.0, ex);
+    for (int j = 0; j < N - 1; j++)
+        tab[wib][j][lane] = live ? dc{df_from(2.0 * Ar[lane * N + j] * rs),
+                                      df_from(2.0 * Ai[lane * N + j] * rs)}
+                                 : dc{{0.f, 0.f}, {0.f, 0.f}};
+    __syncwarp();
+    double sre = 0, cre = 0, sim = 0, cim = 0, asum = 0;
+    const int log_block = a.log_block < (N - 1) ? a.log_block : (N - 1);
+    const uint64_t block_len = 1ull << log_block;
+    bool aborted = false;
+    for (uint64_t g0 = g_begin; g0 < g_end; g0 += block_len) {
+        if (*a.abort_flag) { aborted = true; break; }
+        dc s;
+        {
+            const uint64_t gr = g0 ^ (g0 >> 1);
+            double vr = 0, vi = 0;
+            if (live)
+                for (int j = 0; j < N; j++) {
+                    const bool neg = j < N - 1 && ((gr >> j) & 1);
+                    vr += neg ? -Ar[lane * N + j] * rs : Ar[lane * N + j] * rs;
+                    vi += neg ? -Ai[lane * N + j] * rs : Ai[lane * N + j] * rs;
+                }
+            s = live ? dc{df_from(vr), df_from(vi)} : dc{{1.f, 0.f}, {0.f, 0.f}};
+        }
+        dc blk = dc{{0.f, 0.f}, {0.f, 0.f}};
+        float blk_abs = 0.f;
+        for (uint64_t g = g0; g < g0 + block_len; g++) {
+            if (g != g0) {
+                const int j = __ffsll((long long)g) - 1;
+                const bool sub = ((g >> (j + 1)) & 1) == 0;
+                const dc d = tab[wib][j][lane];
+                if (live) {
+                    s.re = df_add(s.re, sub ? df_neg(d.re) : d.re);
+                    s.im = df_add(s.im, sub ? df_neg(d.im) : d.im);
+                }
+            }
+            dc T = s;
+#pragma unroll
+            for (int lv = 0; lv < LEV; lv++) {
+                const dc o = dc{df_shfl_xor(T.re, 1 << lv), df_shfl_xor(T.im, 1 << lv)};
+                T = dc_mul(T, o);
+            }
+            if (g & 1) { T.re = df_neg(T.re); T.im = df_neg(T.im); }
+            blk.re = df_add(blk.re, T.re);
+            blk.im = df_add(blk.im, T.im);
+            blk_abs += hypotf(T.re.hi, T.im.hi);
+        }
+        kahan(sre, cre, df_to(blk.re));
+        kahan(sim, cim, df_to(blk.im));
+        asum += (double)blk_abs;
+    }
+    if (lane == 0) {
+        double *slot = a.slots + (size_t)gw * 8;
+        slot[0] = sre; slot[1] = cre; slot[2] = sim; slot[3] = cim; slot[4] = asum;
+        if (aborted) atomicExch(a.status, 1);
+    }
+}
+
+__global__ void glynn_c64_reduce(const double *Are, const double *Aim, const double *slots,
+                                 int n, int log_w, double *per_re, double *per_im,
+                                 double *abs_sum) {
+    const int b = blockIdx.x;
+    if (threadIdx.x != 0) return;
+    int et = 0;
+    for (int i = 0; i < n; i++) {
+        double rowsum = 0.0;
+        for (int j = 0; j < n; j++)
+            rowsum += fabs(Are[(size_t)b * n * n + i * n + j]) + fabs(Aim[(size_t)b * n * n + i * n + j]);
+        int e = 0;
+        if (rowsum > 0.0) { frexp(rowsum, &e); e = -e; }
+        et += e;
+    }
+    double sr = 0, cr = 0, si = 0, ci = 0, as = 0;
+    for (int w = 0; w < (1 << log_w); w++) {
+        const double *sl = slots + ((size_t)b * (1 << log_w) + w) * 8;
+        kahan(sr, cr, sl[0]); kahan(sr, cr, -sl[1]);
+        kahan(si, ci, sl[2]); kahan(si, ci, -sl[3]);
+        as += sl[4];
+    }
+    per_re[b] = ldexp(sr, -et - (n - 1));
+    per_im[b] = ldexp(si, -et - (n - 1));
+    if (abs_sum) abs_sum[b] = ldexp(as, -et - (n - 1));
+}
+
+static cudaError_t launch_c64_any(int n, const C64Args &a, cudaStream_t s) {
+    const long warps = (long)a.batch << a.log_w;
+    const unsigned grid = (unsigned)((warps + 3) / 4);
+    switch (n) {
+#define PG_C64_CASE(NN) case NN: glynn_c64_kernel<NN><<<grid, 128, 0, s>>>(a); break;
+        PG_C64_CASE(2) PG_C64_CASE(3) PG_C64_CASE(4) PG_C64_CASE(5) PG_C64_CASE(6)
+        PG_C64_CASE(7) PG_C64_CASE(8) PG_C64_CASE(9) PG_C64_CASE(10) PG_C64_CASE(11)
+        PG_C64_CASE(12) PG_C64_CASE(13) PG_C64_CASE(14) PG_C64_CASE(15) PG_C64_CASE(16)
+        PG_C64_CASE(17) PG_C64_CASE(18) PG_C64_CASE(19) PG_C64_CASE(20) PG_C64_CASE(21)
+        PG_C64_CASE(22) PG_C64_CASE(23) PG_C64_CASE(24) PG_C64_CASE(25) PG_C64_CASE(26)
+        PG_C64_CASE(27) PG_C64_CASE(28) PG_C64_CASE(29) PG_C64_CASE(30) PG_C64_CASE(31)
+        PG_C64_CASE(32)
+#undef PG_C64_CASE
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace pg
+
+extern "C" int pg_glynn_c64_dev(const double *Are, const double *Aim, int batch, int n,
+                                double *per_re, double *per_im, double *abs_sum, void *stream) {
+    using namespace pg;
+    if (batch < 0 || n < 2 || n > 32) return fail(PG_ERANGE, "complex FP64 engine supports 2 <= n <= 32");
+    if (batch == 0) return PG_OK;
+    if (!Are || !Aim || !per_re || !per_im) return fail(PG_EINVAL, "null argument");
+    DeviceInfo dev;
+    int st = device_info(&dev);
+    if (st != PG_OK) return st;
+    volatile int *abort_dev;
+    st = abort_flag_device(&abort_dev);
+    if (st != PG_OK) return st;
+    const int log_states = n - 1;
+    int log_w = 0;
+    while ((((long)batch << log_w) < (long)dev.sm_count * 80) && log_states - (log_w + 1) >= 12)
+        log_w++;
+    const size_t bytes = ((size_t)batch << log_w) * 8 * sizeof(double) + 256;
+    Workspace *ws;
+    st = workspace(&ws, bytes, 64);
+    if (st != PG_OK) return st;
+    cudaStream_t s = stream ? (cudaStream_t)stream : ws->stream;
+    int *status = (int *)((char *)ws->dev + bytes - 256);
+    PG_CUDA(cudaMemsetAsync(ws->dev, 0, bytes, s));
+    C64Args a;
+    a.Are = Are; a.Aim = Aim; a.batch = batch; a.log_w = log_w;
+    a.log_block = std::min(12, log_states - log_w);
+    a.slots = (double *)ws->dev;
+    a.abort_flag = abort_dev;
+    a.status = status;
+    PG_CUDA(launch_c64_any(n, a, s));
+    glynn_c64_reduce<<<batch, 32, 0, s>>>(Are, Aim, (const double *)ws->dev, n, log_w,
+                                          per_re, per_im, abs_sum);
+    PG_CUDA(cudaGetLastError());
+    int hstatus = 0;
+    PG_CUDA(cudaMemcpyAsync(&hstatus, status, sizeof(int), cudaMemcpyDeviceToHost, s));
+    PG_CUDA(cudaStreamSynchronize(s));
+    if (hstatus) return fail(PG_EABORT, "complex FP64 launch aborted by pg_abort()");
+    return PG_OK;
+}

@@ -71,6 +71,8 @@ SIGNATURES = {
                                    ctypes.c_int),
     "pg_exact_partial": ([_c_i64p, ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64, _c_i64p,
                           ctypes.c_int, _c_intp], ctypes.c_int),
+    "pg_glynn_c64_dev": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "pg_glynn_f64_dev": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
 }

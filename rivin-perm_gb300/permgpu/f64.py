@@ -120,27 +120,64 @@ def __getattr__(name):
     raise AttributeError(name)
 
 
-def permanent_float(matrix) -> float:
-    """perm_float.permanent_float API for a real square matrix (FP64)."""
+def permanent_c64(A):
+    """(per, abs_sum) for a (batch, n, n) complex128 CUDA tensor (forward)."""
+    import torch
+    if A.dtype != torch.complex128 or not A.is_cuda:
+        raise TypeError("A must be a complex128 CUDA tensor")
+    if A.dim() < 2 or A.shape[-1] != A.shape[-2]:
+        raise ValueError("A must have shape (..., n, n)")
+    lead = A.shape[:-2]
+    n = A.shape[-1]
+    batch = 1
+    for d in lead:
+        batch *= int(d)
+    Ab = A.reshape(batch, n, n)
+    re = Ab.real.contiguous()
+    im = Ab.imag.contiguous()
+    pr = torch.empty(batch, dtype=torch.float64, device=A.device)
+    pi = torch.empty_like(pr)
+    s = torch.empty_like(pr)
+    if n == 0:
+        pr.fill_(1.0), pi.fill_(0.0), s.fill_(1.0)
+    elif n == 1:
+        pr.copy_(re[:, 0, 0]), pi.copy_(im[:, 0, 0]), s.copy_(Ab[:, 0, 0].abs())
+    elif batch:
+        stream = torch.cuda.current_stream(A.device).cuda_stream
+        _lib.check(_lib.load().pg_glynn_c64_dev(re.data_ptr(), im.data_ptr(), batch, n,
+                                                pr.data_ptr(), pi.data_ptr(), s.data_ptr(),
+                                                stream or None))
+    return torch.complex(pr, pi).reshape(lead), s.reshape(lead)
+
+
+def permanent_float(matrix):
+    """perm_float.permanent_float API (perm_float.py:353-370) for a real or
+    complex square matrix (FP64 / complex128)."""
     import torch
     a = np.asarray(matrix)
-    if np.iscomplexobj(a):
-        raise TypeError("complex matrices are not supported by the GPU FP64 engine")
-    a = np.ascontiguousarray(a, dtype=np.float64)
     if a.ndim != 2 or a.shape[0] != a.shape[1]:
         raise ValueError("Expected a square 2-D matrix")
-    t = torch.from_numpy(a).cuda()
+    if np.iscomplexobj(a):
+        t = torch.from_numpy(np.ascontiguousarray(a, dtype=np.complex128)).cuda()
+        per, _ = permanent_c64(t[None])
+        return complex(per[0].item())
+    t = torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).cuda()
     per, _, _, _ = permanent_f64(t[None], want_grad=False)
     return float(per[0].item())
 
 
-def permanent_gpu(matrix, real: Optional[bool] = None) -> float:
-    """perm_parallel.permanent_gpu API (real matrices)."""
-    a = np.asarray(matrix)
-    if real is False or np.iscomplexobj(a):
-        raise TypeError("complex matrices are not supported by the GPU FP64 engine")
+def permanent_gpu(matrix, real: Optional[bool] = None):
+    """perm_parallel.permanent_gpu API (perm_parallel.py:104-164)."""
+    a = np.asarray(matrix, order="C")
     if a.ndim != 2 or a.shape[0] != a.shape[1]:
         raise ValueError(f"Expected a square 2-D matrix, got shape {a.shape}")
+    is_complex = np.iscomplexobj(a)
+    if real is None:
+        real = not is_complex
+    if real and is_complex:
+        raise ValueError("Cannot use real kernel on complex matrix")
     if a.shape[0] == 0:
-        return 1.0
-    return permanent_float(a)
+        return 1.0 if real else 1.0 + 0.0j
+    if real:
+        return permanent_float(a.astype(np.float64))
+    return permanent_float(a.astype(np.complex128))

@@ -179,7 +179,13 @@ def main():
     for n in (2, 3, 5, 8, 10, 12):
         a = rng.normal(0, 1 / np.sqrt(n), (n, n))
         fl.append({"matrix": a.tolist(), "permanent": float(perm_float.permanent_float(a))})
-    dump("float_small.json", {"source": "perm_float.permanent_float (Ryser + Kahan)", "cases": fl})
+    cx = []
+    for n in (2, 3, 5, 8, 10):
+        a = rng.normal(0, 1 / np.sqrt(2 * n), (n, n)) + 1j * rng.normal(0, 1 / np.sqrt(2 * n), (n, n))
+        v = complex(perm_float.permanent_float(a))
+        cx.append({"re": a.real.tolist(), "im": a.imag.tolist(), "permanent": [v.real, v.imag]})
+    dump("float_small.json", {"source": "perm_float.permanent_float (Ryser + Kahan)", "cases": fl,
+                              "complex_cases": cx})
 
     if args.slow and not (HERE / "exact_generic32.json").exists():
         a = workloads.generic32()

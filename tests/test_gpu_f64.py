@@ -106,6 +106,23 @@ def test_autograd_function(lib):
     assert per.shape == (4,)
 
 
+def test_complex_forward_matches_reference_and_oracle(lib):
+    import torch
+    from permgpu.f64 import permanent_c64, permanent_gpu
+    for c in json.loads((GOLDEN / "float_small.json").read_text())["complex_cases"]:
+        a = np.array(c["re"]) + 1j * np.array(c["im"])
+        per, s = permanent_c64(torch.as_tensor(a).cuda()[None])
+        assert abs(per.item() - complex(*c["permanent"])) <= TOL * s.item()
+        assert abs(permanent_gpu(a) - complex(*c["permanent"])) <= TOL * s.item()
+    rng = np.random.default_rng(41)
+    for n in (13, 20):
+        a = rng.normal(0, 0.2, (n, n)) + 1j * rng.normal(0, 0.2, (n, n))
+        per, s = permanent_c64(torch.as_tensor(a).cuda()[None])
+        want, ws = oracle.glynn_c64(a)
+        assert abs(per.item() - want) <= TOL * s.item()
+        assert abs(s.item() - ws) <= 1e-5 * ws
+
+
 def test_small_orders_and_shapes(lib):
     import torch
     from permgpu.f64 import permanent_f64, permanent_float, permanent_gpu

@@ -57,6 +57,13 @@ def test_float_oracle_matches_reference_float_code():
         assert abs(v - c["permanent"]) <= 1e-12 * max(1.0, s)
 
 
+def test_complex_float_oracle_matches_reference_float_code():
+    for c in golden("float_small.json")["complex_cases"]:
+        a = np.array(c["re"]) + 1j * np.array(c["im"])
+        v, s = oracle.glynn_c64(a)
+        assert abs(v - complex(*c["permanent"])) <= 1e-12 * max(1.0, s)
+
+
 def test_float_gradient_oracle_is_minor_permanent():
     rng = np.random.default_rng(3)
     a = rng.integers(-2, 3, (7, 7))
