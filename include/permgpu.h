@@ -77,6 +77,32 @@ int pg_schur_residues(int n, const uint64_t *primes, const uint64_t *omegas,
                       int k, uint64_t *out);
 
 /*
+ * Schur residues with an explicit evaluation method.  PG_SCHUR_AUTO is
+ * pg_schur_residues: the necklace quotient wherever it applies, else the
+ * Glynn cofactor minor, else the full matrix.  PG_SCHUR_GLYNN forces the
+ * cofactor minor (2^(n-2) Glynn states).  PG_SCHUR_NECKLACE requires the
+ * necklace preconditions (odd prime n < 64, odd modulus < 2^31,
+ * omega^n == 1) for every modulus and returns PG_ERANGE otherwise: the
+ * (n-1)x(n-1) cofactor minor is circulant in primitive-root order and its
+ * 2^(n-1) Glynn sign words collapse to rotation+complement orbits, about
+ * 2^(n-1)/(2(n-1)) terms.  Replaces the necklace branch of
+ * perm_c_ext.schur_permanent_mod_p (perm_c_omp.c:977-1012; enumeration
+ * :89-153, minor :193-226, evaluation :228-305, :416-507) and
+ * schur_necklace_modp_cuda (perm_modp_cuda.cu:957-1090, kernel :524-705).
+ */
+enum pg_schur_method { PG_SCHUR_AUTO = 0, PG_SCHUR_GLYNN = 1, PG_SCHUR_NECKLACE = 2 };
+int pg_schur_residues_method(int n, const uint64_t *primes, const uint64_t *omegas,
+                             int k, int method, uint64_t *out);
+
+/*
+ * Necklace quotient statistics for an odd prime order 3 <= n < 64:
+ * number of orbit representatives and the number of sign words they cover
+ * (2^(n-1) when the quotient is complete).  Host only, no GPU needed.
+ * Replaces perm_c_ext.schur_necklace_orbit_stats (perm_c_omp.c:1062-1082).
+ */
+int pg_necklace_orbit_stats(int n, uint64_t *representatives, uint64_t *words);
+
+/*
  * Binary residues: out[t] = per(A) mod primes[t] for a 0/1 matrix.
  * Contract of perm_binary_ext.binary_permanent_mod_p (perm_binary_omp.c:
  * 386-519) and binary_permanent_modp_cuda (perm_binary_cuda.cu:471-482):

@@ -98,4 +98,12 @@ int glynn_residues_odd(const uint64_t *mats, int n, const uint64_t *moduli,
 // Ryser in Z/2^64 (wrap-around) for the power-of-two part of even moduli.
 int ryser_wrap64(const int64_t *A, int n, uint64_t *out);
 
+// ---- necklace quotient for Schur permanents of prime order (pg_necklace.cu)
+// True when n - 1 is a compiled necklace minor order (n an odd prime < 64).
+bool necklace_supported(int n);
+// out[t] = perm(S_n) mod primes[t] for odd primes[t] < 2^31 with
+// omegas[t]^n == 1; n must satisfy necklace_supported(n).
+int schur_necklace_residues(int n, const uint64_t *primes, const uint64_t *omegas, int k,
+                            uint64_t *out);
+
 }  // namespace pg

@@ -495,19 +495,38 @@ int pg_residues(const int64_t *A, int n, const uint64_t *moduli, int k,
 
 int pg_schur_residues(int n, const uint64_t *primes, const uint64_t *omegas,
                       int k, uint64_t *out) {
+    return pg_schur_residues_method(n, primes, omegas, k, PG_SCHUR_AUTO, out);
+}
+
+int pg_schur_residues_method(int n, const uint64_t *primes, const uint64_t *omegas,
+                             int k, int method, uint64_t *out) {
     using namespace pg;
     if (n < 0 || n >= 64) return fail(PG_ERANGE, "n must satisfy 0 <= n < 64");
     if (k > 0 && (!omegas || !out)) return fail(PG_EINVAL, "null argument");
+    if (method != PG_SCHUR_AUTO && method != PG_SCHUR_GLYNN && method != PG_SCHUR_NECKLACE)
+        return fail(PG_EINVAL, "unknown Schur method");
     int st = check_moduli(primes, k);
     if (st != PG_OK) return st;
     std::vector<uint64_t> minor_mod, minor_mats;
     std::vector<int> minor_of(k, -1);
+    std::vector<uint64_t> neck_p, neck_w;
+    std::vector<int> neck_of;
     for (int t = 0; t < k; t++) {
         const uint64_t p = primes[t];
         if (n <= 1) { out[t] = 1 % p; continue; }
         if (p == 1) { out[t] = 0; continue; }
         const uint64_t w = omegas[t] % p;
-        if (n >= 3 && (n & 1) && (p & 1) && powmod_u64(w, (uint64_t)n, p) == 1 % p) {
+        const bool cofactor =
+            n >= 3 && (n & 1) && (p & 1) && powmod_u64(w, (uint64_t)n, p) == 1 % p;
+        const bool necklace = cofactor && necklace_supported(n) && p < (1ull << 31);
+        if (method == PG_SCHUR_NECKLACE && !necklace)
+            return fail(PG_ERANGE, "necklace quotient needs an odd prime n < 64, an odd "
+                                   "modulus below 2^31 and omega^n == 1");
+        if (necklace && method != PG_SCHUR_GLYNN) {
+            neck_of.push_back(t);
+            neck_p.push_back(p);
+            neck_w.push_back(w);
+        } else if (cofactor) {
             // n * per(minor), minor[r][c] = w^((r+1)(c+1)), (n-1) x (n-1)
             const int q = n - 1;
             minor_of[t] = (int)minor_mod.size();
@@ -547,6 +566,13 @@ int pg_schur_residues(int n, const uint64_t *primes, const uint64_t *omegas,
         for (int t = 0; t < k; t++)
             if (minor_of[t] >= 0)
                 out[t] = mulmod_u64(res[minor_of[t]], (uint64_t)n % primes[t], primes[t]);
+    }
+    if (!neck_p.empty()) {
+        std::vector<uint64_t> res(neck_p.size());
+        st = schur_necklace_residues(n, neck_p.data(), neck_w.data(), (int)neck_p.size(),
+                                     res.data());
+        if (st != PG_OK) return st;
+        for (size_t i = 0; i < neck_of.size(); i++) out[neck_of[i]] = res[i];
     }
     return PG_OK;
 }

@@ -50,6 +50,9 @@ SIGNATURES = {
     "pg_clear_abort": ([], None),
     "pg_residues": ([_c_i64p, ctypes.c_int, _c_u64p, ctypes.c_int, _c_u64p], ctypes.c_int),
     "pg_schur_residues": ([ctypes.c_int, _c_u64p, _c_u64p, ctypes.c_int, _c_u64p], ctypes.c_int),
+    "pg_schur_residues_method": ([ctypes.c_int, _c_u64p, _c_u64p, ctypes.c_int, ctypes.c_int,
+                                  _c_u64p], ctypes.c_int),
+    "pg_necklace_orbit_stats": ([ctypes.c_int, _c_u64p, _c_u64p], ctypes.c_int),
     "pg_binary_residues": ([_c_u8p, ctypes.c_int, _c_u64p, ctypes.c_int, _c_u64p], ctypes.c_int),
     "pg_exact_permanent": ([_c_i64p, ctypes.c_int, _c_u32p, ctypes.c_int], ctypes.c_int),
     "pg_exact_supported": ([_c_i64p, ctypes.c_int], ctypes.c_int),
@@ -146,13 +149,31 @@ def residues(matrix: np.ndarray, moduli) -> list[int]:
     return [int(x) for x in out]
 
 
-def schur_residues(n: int, primes, omegas) -> list[int]:
+SCHUR_METHODS = {"auto": 0, "glynn": 1, "necklace": 2}
+
+
+def schur_residues(n: int, primes, omegas, method: str = "auto") -> list[int]:
+    """perm(S_n) mod each prime; method "auto" | "glynn" | "necklace"."""
+    if method not in SCHUR_METHODS:
+        raise ValueError(f"unknown Schur method {method!r}")
     ps = np.ascontiguousarray(np.asarray(list(primes), dtype=np.uint64))
     ws = np.ascontiguousarray(np.asarray(list(omegas), dtype=np.uint64))
     out = np.zeros(len(ps), dtype=np.uint64)
-    check(load().pg_schur_residues(int(n), ptr(ps, ctypes.c_uint64), ptr(ws, ctypes.c_uint64),
-                                   len(ps), ptr(out, ctypes.c_uint64)))
+    check(load().pg_schur_residues_method(int(n), ptr(ps, ctypes.c_uint64),
+                                          ptr(ws, ctypes.c_uint64), len(ps),
+                                          SCHUR_METHODS[method], ptr(out, ctypes.c_uint64)))
     return [int(x) for x in out]
+
+
+def necklace_orbit_stats(n: int) -> tuple[int, int]:
+    """(representatives, covered sign words) of the necklace quotient for an
+    odd prime order 3 <= n < 64 (host only)."""
+    reps, words = ctypes.c_uint64(), ctypes.c_uint64()
+    st = load().pg_necklace_orbit_stats(int(n), ctypes.byref(reps), ctypes.byref(words))
+    if st == PG_ERANGE:
+        raise ValueError(load().pg_last_error().decode())
+    check(st)
+    return int(reps.value), int(words.value)
 
 
 def binary_residues(matrix: np.ndarray, primes) -> list[int]:

@@ -97,6 +97,12 @@ class GpuExt:
             return 0
         return _lib.schur_residues(n, [p], [omega % p])[0]
 
+    def schur_necklace_orbit_stats(self, n):
+        """(representatives, covered sign words) of the necklace quotient;
+        perm_c_omp.c:1062-1082 semantics (ValueError unless n is an odd
+        prime with 3 <= n < 64).  Host only."""
+        return _lib.necklace_orbit_stats(_parse_int(n, "n"))
+
     def get_max_threads(self):
         return self._threads
 

@@ -40,7 +40,10 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
     ap.add_argument("--slow", action="store_true")
+    ap.add_argument("--necklace-only", action="store_true",
+                    help="regenerate only necklace_stats.json")
     args = ap.parse_args()
+
     ref = Path(args.reference)
     sys.path.insert(0, str(REPO / "oracle" / "_ref"))
     sys.path.insert(0, str(ref))
@@ -54,6 +57,17 @@ def main():
     from permgpu import workloads
 
     assert perm.HAS_C_EXT and perm_binary.HAS_BINARY_EXT
+
+    # ---- necklace quotient statistics (tests/test_schur_cpu_glynn.py:120-130
+    #      checks the same counts against Burnside's lemma) -------------------
+    stats = {}
+    for n in (3, 5, 7, 11, 13, 17, 19, 23, 29, 31):
+        reps, words = perm_c_ext.schur_necklace_orbit_stats(n)
+        stats[str(n)] = [reps, words]
+    dump("necklace_stats.json", {"source": "perm_c_ext.schur_necklace_orbit_stats(n)",
+                                 "stats": stats})
+    if args.necklace_only:
+        return
 
     # ---- generic residues across modulus tiers (tests/test_generic_native.py
     #      uses the same tiers and random.Random seeds) ----------------------

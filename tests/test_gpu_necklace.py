@@ -1,0 +1,75 @@
+"""GPU checks of the necklace quotient for Schur permanents of prime order.
+
+The necklace kernel must give exactly the residues of the Glynn cofactor
+path (itself checked against the oracle) and of the oracle, and the CRT of
+its residues must reproduce the reference's published perm(S_n) table.
+"""
+
+import json
+
+import pytest
+
+import oracle
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+
+def _plan(n):
+    from permgpu.crt import nth_root_of_unity, plan_schur
+    primes, congruence, bound = plan_schur(n)
+    return primes, [nth_root_of_unity(n, p) for p in primes], congruence, bound
+
+
+@pytest.mark.parametrize("n", [3, 5, 7, 11, 13, 17, 19])
+def test_necklace_matches_oracle(lib, n):
+    from permgpu import _lib
+    primes, omegas, _, _ = _plan(n)
+    # extra moduli: small primes = 1 mod n and the trivial root omega = 1
+    extra = [p for p in range(n + 1, 4000, n) if oracle._is_prime(p)][:3]
+    ps = list(primes) + extra + extra[:1]
+    ws = list(omegas) + [pow(2, (p - 1) // n, p) for p in extra] + [1]
+    got = _lib.schur_residues(n, ps, ws, method="necklace")
+    for p, w, r in zip(ps, ws, got):
+        assert r == oracle.schur_mod_p(n, w, p, 8), (n, p, w)
+
+
+@pytest.mark.parametrize("n", [23, 29])
+def test_necklace_matches_glynn_cofactor_path(lib, n):
+    from permgpu import _lib
+    primes, omegas, _, _ = _plan(n)
+    a = _lib.schur_residues(n, primes, omegas, method="necklace")
+    b = _lib.schur_residues(n, primes, omegas, method="glynn")
+    assert a == b
+
+
+@pytest.mark.parametrize("n", [23, 29, 31, 37, 41])
+def test_schur_table_through_necklace(lib, n):
+    # full-size property: the CRT of necklace residues is the published value
+    from permgpu import _lib
+    from permgpu.crt import crt
+    table = json.loads((GOLDEN / "schur.json").read_text())["table"]
+    primes, omegas, congruence, bound = _plan(n)
+    res = _lib.schur_residues(n, primes, omegas, method="necklace")
+    moduli = list(primes)
+    if congruence:
+        res.append(congruence[0])
+        moduli.append(congruence[1])
+    x = crt(res, moduli)
+    m = 1
+    for q in moduli:
+        m *= q
+    if x > bound:
+        x -= m
+    assert x == int(table[str(n)])
+
+
+def test_auto_method_uses_necklace_and_rejects_nothing(lib):
+    from permgpu import _lib
+    primes, omegas, _, _ = _plan(19)
+    assert _lib.schur_residues(19, primes, omegas) == _lib.schur_residues(
+        19, primes, omegas, method="necklace")
+    # a modulus above 2^31 falls back to the Glynn minor under "auto"
+    p = 4294967161
+    w = 2662262
+    assert _lib.schur_residues(33, [p], [w]) == [1428739342]

@@ -134,3 +134,37 @@ def test_normalize_binary_strict():
     assert pb.normalize_binary_matrix([[2, 0], [0, -1]], strict=False) == ((1, 0), (0, 1))
     with pytest.raises(TypeError):
         pb.normalize_binary_matrix([[0.5]])
+
+
+def _burnside_rotation_complement(length):
+    # orbits of {0,1}^length under rotation and complement
+    divisors = [d for d in range(1, length + 1) if length % d == 0]
+    phi = lambda d: sum(1 for k in range(1, d + 1) if math.gcd(k, d) == 1)
+    rot = sum(phi(d) * 2 ** (length // d) for d in divisors)
+    comp = sum(phi(d) * 2 ** (length // d) for d in divisors if d % 2 == 0)
+    return (rot + comp) // (2 * length)
+
+
+def test_necklace_orbit_stats_match_reference():
+    # the device walker, run on the host, against the reference's counts
+    ext = GpuExt()
+    for n, (reps, words) in golden("necklace_stats.json")["stats"].items():
+        assert ext.schur_necklace_orbit_stats(int(n)) == (reps, words)
+    for n in (3, 5, 7, 11, 13, 17, 19, 23):
+        reps, words = ext.schur_necklace_orbit_stats(n)
+        assert reps == _burnside_rotation_complement(n - 1) and words == 1 << (n - 1)
+    for bad in (0, 2, 9, 25, 64):
+        with pytest.raises(ValueError, match="odd prime"):
+            ext.schur_necklace_orbit_stats(bad)
+
+
+def test_schur_necklace_method_rejects_unsupported_inputs():
+    from permgpu import _lib
+    with pytest.raises(_lib.PermGpuError, match="PG_ERANGE"):
+        _lib.schur_residues(9, [19], [pow(2, 2, 19)], method="necklace")       # n not prime
+    with pytest.raises(_lib.PermGpuError, match="PG_ERANGE"):
+        _lib.schur_residues(11, [4294967311], [1], method="necklace")          # p >= 2^31
+    with pytest.raises(_lib.PermGpuError, match="PG_ERANGE"):
+        _lib.schur_residues(11, [23], [5], method="necklace")                  # 5^11 != 1 mod 23
+    with pytest.raises(ValueError):
+        _lib.schur_residues(11, [23], [1], method="ryser")
