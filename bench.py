@@ -507,6 +507,15 @@ def run_gpu_float28(args, world, rank, local):
         }))
 
 
+def necklace_representatives(length: int) -> int:
+    """Orbits of {0,1}^length under rotation and complement (Burnside)."""
+    phi = lambda d: sum(1 for k in range(1, d + 1) if math.gcd(k, d) == 1)
+    divisors = [d for d in range(1, length + 1) if length % d == 0]
+    rot = sum(phi(d) * 2 ** (length // d) for d in divisors)
+    comp = sum(phi(d) * 2 ** (length // d) for d in divisors if d % 2 == 0)
+    return (rot + comp) // (2 * length)
+
+
 def run_gpu_exact_set(args, world, rank, local):
     """schur: exact perm(S_31) and perm(S_33) (residue engine, primes == 1 mod
     n, below 2^31, Graham-Lehmer congruence at CRT time); binary40: eight
@@ -528,6 +537,17 @@ def run_gpu_exact_set(args, world, rank, local):
             return [permgpu.permanent(n) for n in items]
         want = [int(table[str(n)]) for n in items]
         desc = "perm(S_31), perm(S_33): (n-1)x(n-1) minors, primes == 1 (mod n) < 2^31"
+    elif args.workload == "schur41":
+        # prime order: the 40x40 circulant minor through the necklace quotient;
+        # "states" counts orbit representatives evaluated (times primes)
+        items = [41]
+        states = len(plan_schur(41)[0]) * necklace_representatives(40)
+
+        def step():
+            return [permgpu.permanent(n) for n in items]
+        want = [int(table["41"])]
+        desc = ("perm(S_41): 40x40 circulant cofactor minor, rotation+complement necklace "
+                "representatives, primes == 1 (mod 41) < 2^31")
     else:
         mats = workloads.binary40(8)
         items = [m.tolist() for m in mats]
@@ -554,7 +574,21 @@ def run_gpu_exact_set(args, world, rank, local):
     barrier(world)
     clk = clocks.stop()
     step_s = max_over_ranks(world, statistics.mean(ts))
-    if rank == 0:
+    if rank == 0 and args.workload == "schur41":
+        print(json.dumps({
+            "metric": "seconds to exact perm(S_41)", "value": step_s, "unit": "s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * step_s, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int32", "data": "none (the matrix is S_41)",
+            "config": {"workload": f"{args.workload}: {desc}", "representatives": states},
+            "representatives_per_s": states / step_s, "results": [str(v) for v in got],
+            "result_checked_against_reference": True,
+            "e2e": {"value": step_s, "unit": "s", "h2d_bytes_per_step": None,
+                    "d2h_bytes_per_step": None,
+                    "note": "whole-call API permgpu.permanent(41) timed end to end"},
+            "clocks": clk,
+        }))
+    elif rank == 0:
         print(json.dumps({
             "metric": f"Glynn steps/s ({args.workload})", "value": world * states / step_s,
             "unit": "steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -577,7 +611,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="generic32",
-                    choices=sorted(WORKLOADS) + ["batch4096", "float28", "schur", "binary40"])
+                    choices=sorted(WORKLOADS) + ["batch4096", "float28", "schur", "schur41",
+                                                 "binary40"])
     ap.add_argument("--residue-loop-sample", type=int, default=256)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -591,7 +626,7 @@ def main():
         run_gpu_batch(args, world, rank, local)
     elif args.workload == "float28":
         run_gpu_float28(args, world, rank, local)
-    elif args.workload in ("schur", "binary40"):
+    elif args.workload in ("schur", "schur41", "binary40"):
         run_gpu_exact_set(args, world, rank, local)
     else:
         run_gpu(args, world, rank, local)

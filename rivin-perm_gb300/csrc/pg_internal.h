@@ -99,10 +99,15 @@ int glynn_residues_odd(const uint64_t *mats, int n, const uint64_t *moduli,
 int ryser_wrap64(const int64_t *A, int n, uint64_t *out);
 
 // ---- necklace quotient for Schur permanents of prime order (pg_necklace.cu)
+// Moduli must be odd and below this bound (lazy row sums, see pg_necklace.cu).
+constexpr uint64_t NECKLACE_PRIME_LIMIT = 1ull << 30;
+// Smallest order the automatic Schur dispatch sends to the necklace kernel;
+// below it the Glynn cofactor kernel finishes first.
+constexpr int NECKLACE_AUTO_MIN_ORDER = 37;
 // True when n - 1 is a compiled necklace minor order (n an odd prime < 64).
 bool necklace_supported(int n);
-// out[t] = perm(S_n) mod primes[t] for odd primes[t] < 2^31 with
-// omegas[t]^n == 1; n must satisfy necklace_supported(n).
+// out[t] = perm(S_n) mod primes[t] for odd primes[t] < NECKLACE_PRIME_LIMIT
+// with omegas[t]^n == 1; n must satisfy necklace_supported(n).
 int schur_necklace_residues(int n, const uint64_t *primes, const uint64_t *omegas, int k,
                             uint64_t *out);
 

@@ -16,6 +16,10 @@ _MR_WITNESSES = (2, 3, 5, 7, 11, 13, 17, 19, 23, 29, 31, 37)
 
 # Odd moduli below this run the 32-bit Montgomery kernel.
 FAST_PRIME_LIMIT = 1 << 31
+# The necklace kernel (Schur permanents of prime order) sums row sums lazily
+# and needs moduli below 2^30; it takes over from order 37 on.
+NECKLACE_PRIME_LIMIT = 1 << 30
+NECKLACE_AUTO_MIN_ORDER = 37
 
 
 def is_prime(n: int) -> bool:
@@ -161,16 +165,25 @@ def nth_root_of_unity(n: int, p: int) -> int:
     return pow(primitive_root(p), (p - 1) // n, p)
 
 
-def plan_schur(n: int) -> Tuple[List[int], Optional[Tuple[int, int]], int]:
-    """GPU Schur plan: primes p == 1 (mod n), p < 2^31, plus the
-    Graham-Lehmer congruence used only at CRT time.  Returns
-    (primes, congruence, bound)."""
+def uses_necklace(n: int) -> bool:
+    """True when the automatic Schur dispatch evaluates perm(S_n) with the
+    necklace quotient: n an odd prime with NECKLACE_AUTO_MIN_ORDER <= n < 64."""
+    return NECKLACE_AUTO_MIN_ORDER <= n < 64 and is_prime(n)
+
+
+def plan_schur(n: int, prime_limit: Optional[int] = None
+               ) -> Tuple[List[int], Optional[Tuple[int, int]], int]:
+    """GPU Schur plan: primes p == 1 (mod n) below `prime_limit` (2^30 for
+    necklace orders, else 2^31), plus the Graham-Lehmer congruence used only
+    at CRT time.  Returns (primes, congruence, bound)."""
+    if prime_limit is None:
+        prime_limit = NECKLACE_PRIME_LIMIT if uses_necklace(n) else FAST_PRIME_LIMIT
     bound = schur_permanent_bound(n)
     target = 2 * bound + 1
     congruence = graham_lehmer_congruence(n)
     if congruence is not None:
         target = -(-target // congruence[1])
-    primes = descending_primes(target, FAST_PRIME_LIMIT, n) if target > 1 else []
+    primes = descending_primes(target, prime_limit, n) if target > 1 else []
     return primes, congruence, bound
 
 

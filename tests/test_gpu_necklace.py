@@ -16,8 +16,9 @@ pytestmark = pytest.mark.gpu
 
 
 def _plan(n):
-    from permgpu.crt import nth_root_of_unity, plan_schur
-    primes, congruence, bound = plan_schur(n)
+    # necklace moduli: primes == 1 (mod n) below 2^30
+    from permgpu.crt import NECKLACE_PRIME_LIMIT, nth_root_of_unity, plan_schur
+    primes, congruence, bound = plan_schur(n, NECKLACE_PRIME_LIMIT)
     return primes, [nth_root_of_unity(n, p) for p in primes], congruence, bound
 
 
@@ -43,7 +44,7 @@ def test_necklace_matches_glynn_cofactor_path(lib, n):
     assert a == b
 
 
-@pytest.mark.parametrize("n", [23, 29, 31, 37, 41])
+@pytest.mark.parametrize("n", [23, 29, 31, 37, 41, 43])
 def test_schur_table_through_necklace(lib, n):
     # full-size property: the CRT of necklace residues is the published value
     from permgpu import _lib
@@ -64,12 +65,19 @@ def test_schur_table_through_necklace(lib, n):
     assert x == int(table[str(n)])
 
 
-def test_auto_method_uses_necklace_and_rejects_nothing(lib):
+def test_auto_method_agrees_with_both_paths(lib):
     from permgpu import _lib
-    primes, omegas, _, _ = _plan(19)
-    assert _lib.schur_residues(19, primes, omegas) == _lib.schur_residues(
-        19, primes, omegas, method="necklace")
-    # a modulus above 2^31 falls back to the Glynn minor under "auto"
-    p = 4294967161
-    w = 2662262
-    assert _lib.schur_residues(33, [p], [w]) == [1428739342]
+    from permgpu.crt import nth_root_of_unity, plan_schur
+    for n in (19, 37):
+        primes, omegas, _, _ = _plan(n)
+        auto = _lib.schur_residues(n, primes, omegas)
+        assert auto == _lib.schur_residues(n, primes, omegas, method="necklace")
+        if n < 37:
+            assert auto == _lib.schur_residues(n, primes, omegas, method="glynn")
+    # a modulus above 2^30 takes the Glynn minor under "auto"
+    primes = plan_schur(37)[0][:1] + [p for p in plan_schur(37, 1 << 31)[0][:1]]
+    omegas = [nth_root_of_unity(37, p) for p in primes]
+    assert _lib.schur_residues(37, primes, omegas)[1] == _lib.schur_residues(
+        37, primes[1:], omegas[1:], method="glynn")[0]
+    # the pinned residue of tests/test_cuda_device_schur_glynn.py:141-146
+    assert _lib.schur_residues(33, [4294967161], [2662262]) == [1428739342]

@@ -163,7 +163,9 @@ def test_schur_necklace_method_rejects_unsupported_inputs():
     with pytest.raises(_lib.PermGpuError, match="PG_ERANGE"):
         _lib.schur_residues(9, [19], [pow(2, 2, 19)], method="necklace")       # n not prime
     with pytest.raises(_lib.PermGpuError, match="PG_ERANGE"):
-        _lib.schur_residues(11, [4294967311], [1], method="necklace")          # p >= 2^31
+        _lib.schur_residues(11, [4294967311], [1], method="necklace")          # p >= 2^30
+    with pytest.raises(_lib.PermGpuError, match="PG_ERANGE"):
+        _lib.schur_residues(11, [2147483629], [1], method="necklace")          # p >= 2^30
     with pytest.raises(_lib.PermGpuError, match="PG_ERANGE"):
         _lib.schur_residues(11, [23], [5], method="necklace")                  # 5^11 != 1 mod 23
     with pytest.raises(ValueError):
