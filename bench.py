@@ -538,16 +538,18 @@ def run_gpu_exact_set(args, world, rank, local):
         want = [int(table[str(n)]) for n in items]
         desc = "perm(S_31), perm(S_33): (n-1)x(n-1) minors, primes == 1 (mod n) < 2^31"
     elif args.workload == "schur41":
-        # prime order: the 40x40 circulant minor through the necklace quotient;
-        # "states" counts orbit representatives evaluated (times primes)
-        items = [41]
-        states = len(plan_schur(41)[0]) * necklace_representatives(40)
+        # prime order (41 unless --order says otherwise): the (n-1)x(n-1)
+        # circulant minor through the necklace quotient; "states" counts the
+        # rotation+complement orbits (times primes)
+        n = args.order
+        items = [n]
+        states = len(plan_schur(n)[0]) * necklace_representatives(n - 1)
 
         def step():
             return [permgpu.permanent(n) for n in items]
-        want = [int(table["41"])]
-        desc = ("perm(S_41): 40x40 circulant cofactor minor, rotation+complement necklace "
-                "representatives, primes == 1 (mod 41) < 2^31")
+        want = [int(table[str(n)])]
+        desc = (f"perm(S_{n}): {n - 1}x{n - 1} circulant cofactor minor, rotation+complement "
+                f"necklace orbits, primes == 1 (mod {n}) < 2^30")
     else:
         mats = workloads.binary40(8)
         items = [m.tolist() for m in mats]
@@ -575,18 +577,23 @@ def run_gpu_exact_set(args, world, rank, local):
     clk = clocks.stop()
     step_s = max_over_ranks(world, statistics.mean(ts))
     if rank == 0 and args.workload == "schur41":
+        n = args.order
+        # published: perm(S_41) by the reference's CUDA necklace kernel in
+        # 47.39 s on a GH200 (README.md:596)
+        published = 47.39 if n == 41 else None
         print(json.dumps({
-            "metric": "seconds to exact perm(S_41)", "value": step_s, "unit": "s",
+            "metric": f"seconds to exact perm(S_{n})", "value": step_s, "unit": "s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * step_s, "higher_is_better": False, "scaling": "weak",
-            "vs_baseline": None, "dtype": "int32", "data": "none (the matrix is S_41)",
-            "config": {"workload": f"{args.workload}: {desc}", "representatives": states},
-            "representatives_per_s": states / step_s, "results": [str(v) for v in got],
+            "vs_baseline": step_s / published if published else None,
+            "dtype": "int32", "data": f"none (the matrix is S_{n})",
+            "config": {"workload": f"{args.workload}: {desc}", "orbits": states},
+            "orbits_per_s": states / step_s, "results": [str(v) for v in got],
             "result_checked_against_reference": True,
             "e2e": {"value": step_s, "unit": "s", "h2d_bytes_per_step": None,
                     "d2h_bytes_per_step": None,
-                    "note": "whole-call API permgpu.permanent(41) timed end to end"},
-            "clocks": clk,
+                    "note": f"whole-call API permgpu.permanent({n}) timed end to end"},
+            "clocks": clk, "gpu_launches": args.steps,
         }))
     elif rank == 0:
         print(json.dumps({
@@ -618,6 +625,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--batch", type=int, default=256,
                     help="float28: matrices per step (256 is the workload; smaller for profiling)")
+    ap.add_argument("--order", type=int, default=41,
+                    help="schur41: prime Schur order (41 is the workload; 37 for profiling)")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":

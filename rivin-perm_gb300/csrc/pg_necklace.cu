@@ -355,6 +355,8 @@ struct NeckArgs {
     int *status;
 };
 
+constexpr int NK_CHAINS = 4;      // Montgomery chains per term
+
 template <int L>
 struct NeckLane {
     static constexpr int LS = nk_stride(L);
@@ -413,9 +415,13 @@ struct NeckLane {
     // byte 0 (< 2p).
     __device__ __forceinline__ void eval(const uint32_t *tab, uint32_t e, uint32_t orbit) {
         const uint32_t *t0 = tab + (e & 0xff) * LS;
-        uint32_t ch[4] = {0, 0, 0, 0};
         uint32_t prod;
         if constexpr (L >= 8) {
+            // C independent Montgomery chains (ILP), joined by a pairwise
+            // tree: (L - C) + (C - 1) = L - 1 reductions in all.  Row sums and
+            // chain values stay below 2p.
+            constexpr int C = L >= 2 * NK_CHAINS ? NK_CHAINS : 4;
+            uint32_t ch[C];
 #pragma unroll
             for (int q = 0; q < L / V; q++) {
                 uint32_t sr[V];
@@ -430,16 +436,16 @@ struct NeckLane {
 #pragma unroll
                 for (int i = 0; i < V; i++) {
                     const int r = V * q + i;
-                    if (r < 4) ch[r] = sr[i];
-                    else ch[r & 3] = m32_redc_mul(ch[r & 3], sr[i], p, pinv);
+                    if (r < C) ch[r] = sr[i];
+                    else ch[r % C] = m32_redc_mul(ch[r % C], sr[i], p, pinv);
                 }
             }
-            // every chain took at least one reduction: ch[i] < 2p
-            const uint32_t c1 = __viaddmin_u32(ch[1], 0u - p, ch[1]);
-            const uint32_t c3 = __viaddmin_u32(ch[3], 0u - p, ch[3]);
-            const uint32_t c01 = m32_redc_mul(ch[0], c1, p, pinv);
-            const uint32_t c23 = m32_redc_mul(ch[2], c3, p, pinv);
-            prod = m32_redc_mul(c01, __viaddmin_u32(c23, 0u - p, c23), p, pinv);
+#pragma unroll
+            for (int w = 1; w < C; w *= 2)
+#pragma unroll
+                for (int i = 0; i + w < C; i += 2 * w)
+                    ch[i] = m32_redc_mul(ch[i], __viaddmin_u32(ch[i + w], 0u - p, ch[i + w]), p, pinv);
+            prod = ch[0];
         } else {
             // L < 8: one byte; reduce each row sum (< 2p) and chain serially
             prod = 0;

@@ -139,7 +139,11 @@ def main():
         "computed": exact_small,
         "residues": schur_res,
         "pins": [{"n": 33, "p": 4294967161, "omega": 2662262, "residue": 1428739342,
-                  "source": "tests/test_cuda_device_schur_glynn.py:141-146"}],
+                  "source": "tests/test_cuda_device_schur_glynn.py:141-146"},
+                 {"n": 41, "p": 4294966153, "omega": 782766686, "residue": 3889040436,
+                  "source": "tests/test_cuda_device_schur_glynn.py:153-160"},
+                 {"n": 47, "p": 4294967161, "omega": 1002938914, "residue": 4173217525,
+                  "source": "tests/test_cuda_device_schur_glynn.py:163-172"}],
         "graham_lehmer": {str(n): list(perm._graham_lehmer_schur_congruence(n) or ())
                           for n in range(3, 48, 2)},
         "cpu_plan_prime_counts": {str(n): len(perm._plan_schur_exact_crt(

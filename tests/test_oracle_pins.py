@@ -110,6 +110,17 @@ def test_schur_table_small_orders_from_oracle_crt():
         assert x == int(table[str(n)])
 
 
+def test_schur_table_agrees_with_reference_gpu_residue_pins():
+    # the reference's CUDA residues for n = 33, 41, 47 (32-bit primes) are the
+    # published perm(S_n) reduced mod those primes; the GPU tests check our
+    # exact perm(S_n) against the same table
+    s = golden("schur.json")
+    for pin in s["pins"]:
+        n, p, w = pin["n"], pin["p"], pin["omega"]
+        assert pow(w, n, p) == 1
+        assert int(s["table"][str(n)]) % p == pin["residue"]
+
+
 def test_float_gradient_oracle_matches_reference_minors():
     # integer-valued 20x20: the reference's exact permanents of all 400
     # minors (perm.matrix_permanent) are the gradient
