@@ -507,6 +507,95 @@ def run_gpu_float28(args, world, rank, local):
         }))
 
 
+def run_gpu_poly(args, world, rank, local):
+    """rook28: exact rook polynomial (matching counts k = 0..28) of a 28x28
+    Bernoulli(0.5) 0/1 matrix, numpy default_rng(28 + rank), through
+    permgpu.rook_polynomial: the coefficients of per(J + x A) modulo every
+    CRT prime (< 2^30) in one launch, CRT, division by (n-k)!.  value =
+    prime-states per second of the residue launch (one state = one Gray sign
+    vector for one prime: the product of 28 linear factors); e2e = the
+    whole rook_polynomial call from host lists to exact integers."""
+    import numpy as np
+    import torch
+    import permgpu
+    from permgpu import _lib, poly
+    torch.cuda.set_device(local)
+    n = 28
+    a = (np.random.default_rng(28 + rank).random((n, n)) < 0.5).astype(np.int64)
+    ones = np.ones((n, n), dtype=np.int64)
+    am = tuple(tuple(int(v) for v in row) for row in a)
+    bounds = poly._bounds(tuple((1,) * n for _ in range(n)), am)
+    primes = poly._gpu_primes(max(bounds))
+    states = len(primes) * (1 << (n - 1))
+    # IMAD-class instructions per state: factor r = 1..n-1 costs two plain
+    # reductions (3 each) and r fused two-product reductions (4 each)
+    imad_per_state = 2 * (n - 1) * (n + 3)
+    for _ in range(args.warmup):
+        got = permgpu.rook_polynomial(a.tolist())
+        _lib.affine_residues(ones, a, primes)
+    if got[1] != int(a.sum()):
+        raise SystemExit("rook polynomial failed its r_1 = #ones check")
+    peak = _lib.probe_int_throughput(0)
+    clocks = ClockSampler(local).start()
+    barrier(world)
+    ts, te = [], []
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        _lib.affine_residues(ones, a, primes)
+        ts.append(time.perf_counter() - t)
+        t = time.perf_counter()
+        res = permgpu.rook_polynomial(a.tolist())
+        te.append(time.perf_counter() - t)
+        if res != got:
+            raise SystemExit("results changed between steps")
+    barrier(world)
+    clk = clocks.stop()
+    step_s = max_over_ranks(world, statistics.mean(ts))
+    e2e_s = max_over_ranks(world, statistics.mean(te))
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import oracle
+        oracle.build()
+        threads = os.cpu_count() or 1
+        t = time.perf_counter()
+        oracle.affine_range_mod_p(ones, a, primes[0], 0, 1 << 14, threads)
+        rate = (1 << 14) / max(time.perf_counter() - t, 1e-6)
+        sample = int(min(1 << (n - 1), max(1 << 14, rate * args.cpu_seconds)))
+        t = time.perf_counter()
+        oracle.affine_range_mod_p(ones, a, primes[0], 0, sample, threads)
+        per_prime = sample / (time.perf_counter() - t)
+        cpu = {"value": per_prime, "unit": "prime-states/s", "cores": threads, "kind": "port",
+               "sample": f"Gray states [0, {sample}) of per(J + xA) for the workload matrix mod "
+                         f"one prime, {threads} OpenMP threads (restatement of "
+                         f"perm_polynomial.py:268-329); the exact vector needs "
+                         f"{len(primes)} primes x 2^{n - 1} states",
+               "time_to_exact_s_est": states / per_prime}
+    if rank == 0:
+        achieved = states * imad_per_state / step_s / 1e12
+        print(json.dumps({
+            "metric": "polynomial Glynn prime-states/s (rook28)", "value": world * states / step_s,
+            "unit": "prime-states/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * step_s, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32 Montgomery",
+            "data": "synthetic",
+            "config": {"workload": "rook28: rook polynomial of a 28x28 Bernoulli(0.5) 0/1 "
+                                   "matrix, numpy default_rng(28)", "crt_primes": len(primes),
+                       "states": states},
+            "time_to_exact_s": e2e_s, "results_r1_rn": [str(got[1]), str(got[-1])],
+            "roofline": {"bound": "imad", "achieved": achieved, "peak": peak, "unit": "Tops/s",
+                         "frac": achieved / peak, "traffic": None,
+                         "peak_source": "measured live: pg_probe_int_throughput mad.lo.u32",
+                         "work_per_state": {"imad_class": imad_per_state}},
+            "cpu_baseline": cpu,
+            "e2e": {"value": world * states / e2e_s, "unit": "prime-states/s",
+                    "h2d_bytes_per_step": 2 * 8 * n * n, "d2h_bytes_per_step": 8 * (n + 1) * len(primes),
+                    "ms_per_step": 1e3 * e2e_s},
+            "clocks": clk, "gpu_launches": 2 * args.steps,
+        }))
+
+
 def necklace_representatives(length: int) -> int:
     """Orbits of {0,1}^length under rotation and complement (Burnside)."""
     phi = lambda d: sum(1 for k in range(1, d + 1) if math.gcd(k, d) == 1)
@@ -619,7 +708,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="generic32",
                     choices=sorted(WORKLOADS) + ["batch4096", "float28", "schur", "schur41",
-                                                 "binary40"])
+                                                 "binary40", "rook28"])
     ap.add_argument("--residue-loop-sample", type=int, default=256)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -637,6 +726,8 @@ def main():
         run_gpu_float28(args, world, rank, local)
     elif args.workload in ("schur", "schur41", "binary40"):
         run_gpu_exact_set(args, world, rank, local)
+    elif args.workload == "rook28":
+        run_gpu_poly(args, world, rank, local)
     else:
         run_gpu(args, world, rank, local)
     if world > 1:

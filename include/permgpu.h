@@ -103,6 +103,19 @@ int pg_schur_residues_method(int n, const uint64_t *primes, const uint64_t *omeg
 int pg_necklace_orbit_stats(int n, uint64_t *representatives, uint64_t *words);
 
 /*
+ * Affine-polynomial residues: out[t*(n+1) + d] = coefficient of x^d in
+ * per(C + x L) mod moduli[t], for row-major n x n signed 64-bit C and L,
+ * 0 <= n <= 32 and odd moduli 3 <= m < 2^30 (they need not be prime).  All
+ * moduli run in one launch.  Replaces perm_polynomial_ext.affine_permanent_mod
+ * (perm_polynomial_omp.c:1207-1360, engine :434-486, :612-779); the
+ * principal-permanent polynomial per(I + x A) and the rook polynomials
+ * per(J + x A) (perm_polynomial.py:1217-1287, :1288-1411, :1512-1606) are
+ * this entry with C = I or C = J.
+ */
+int pg_affine_residues(const int64_t *C, const int64_t *L, int n,
+                       const uint64_t *moduli, int k, uint64_t *out);
+
+/*
  * Binary residues: out[t] = per(A) mod primes[t] for a 0/1 matrix.
  * Contract of perm_binary_ext.binary_permanent_mod_p (perm_binary_omp.c:
  * 386-519) and binary_permanent_modp_cuda (perm_binary_cuda.cu:471-482):

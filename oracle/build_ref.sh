@@ -1,8 +1,9 @@
 #!/usr/bin/env bash
-# Compile the reference's own OpenMP residue extensions (perm_c_omp.c and
-# perm_binary_omp.c) from the reference checkout into oracle/_ref/.  These are
-# CPython extension modules used only as the CPU checker and CPU baseline; no
-# reference source is copied into this repository.
+# Compile the reference's own OpenMP extensions (perm_c_omp.c,
+# perm_binary_omp.c and perm_polynomial_omp.c) from the reference checkout
+# into oracle/_ref/.  These are CPython extension modules used only as the CPU
+# checker, the golden-vector generator and the CPU baseline; no reference
+# source is copied into this repository.
 #
 # usage: oracle/build_ref.sh [REFERENCE_DIR]   (default /root/reference)
 set -euo pipefail
@@ -18,5 +19,7 @@ PYINC="$(python3 -c 'import sysconfig; print(sysconfig.get_paths()["include"])')
 SUFFIX="$(python3 -c 'import sysconfig; print(sysconfig.get_config_var("EXT_SUFFIX"))')"
 gcc -O3 -fopenmp -fPIC -shared -I"$PYINC" "$REF/perm_c_omp.c" -o "$OUT/perm_c_ext$SUFFIX" &
 gcc -O3 -fopenmp -fPIC -shared -I"$PYINC" "$REF/perm_binary_omp.c" -o "$OUT/perm_binary_ext$SUFFIX" &
+gcc -O3 -std=c11 -fopenmp -fPIC -shared -I"$PYINC" "$REF/perm_polynomial_omp.c" \
+    -o "$OUT/perm_polynomial_ext$SUFFIX" &
 wait
-echo "built $OUT/perm_c_ext$SUFFIX $OUT/perm_binary_ext$SUFFIX"
+echo "built $OUT/perm_c_ext$SUFFIX $OUT/perm_binary_ext$SUFFIX $OUT/perm_polynomial_ext$SUFFIX"

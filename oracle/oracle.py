@@ -71,6 +71,11 @@ def load():
         lib.or_glynn_c64.restype = None
         lib.or_max_threads.argtypes = []
         lib.or_max_threads.restype = ctypes.c_int
+        lib.or_affine_mod_p.argtypes = [i64p, i64p, ctypes.c_int, ctypes.c_int64, ctypes.c_int, i64p]
+        lib.or_affine_mod_p.restype = ctypes.c_int
+        lib.or_affine_range_mod_p.argtypes = [i64p, i64p, ctypes.c_int, ctypes.c_int64,
+                                              ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, i64p]
+        lib.or_affine_range_mod_p.restype = ctypes.c_int
         _lib = lib
     return _lib
 
@@ -216,6 +221,66 @@ def glynn_f64_grad(matrix, threads: int = 0) -> np.ndarray:
                              int(threads or max_threads()),
                              g.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
     return g
+
+
+def affine_mod_p(constant, linear, p: int, threads: int = 0) -> list[int]:
+    """Coefficients of per(C + x L) mod odd p, ascending degree (n + 1 of
+    them) — the fixed-sign Glynn of perm_polynomial.py:268-329."""
+    c = _i64(constant)
+    l = _i64(linear)
+    n = c.shape[0] if c.ndim == 2 else 0
+    out = np.zeros(n + 1, dtype=np.int64)
+    p64 = ctypes.POINTER(ctypes.c_int64)
+    st = load().or_affine_mod_p(c.ctypes.data_as(p64), l.ctypes.data_as(p64), n, int(p),
+                                int(threads or max_threads()), out.ctypes.data_as(p64))
+    if st != 0:
+        raise RuntimeError("oracle failed")
+    return [int(x) for x in out]
+
+
+def affine_range_mod_p(constant, linear, p: int, lo: int, hi: int, threads: int = 0) -> list[int]:
+    """Unscaled partial coefficient sums over Gray states [lo, hi) mod odd p."""
+    c = _i64(constant)
+    l = _i64(linear)
+    n = c.shape[0]
+    out = np.zeros(n + 1, dtype=np.int64)
+    p64 = ctypes.POINTER(ctypes.c_int64)
+    st = load().or_affine_range_mod_p(c.ctypes.data_as(p64), l.ctypes.data_as(p64), n, int(p),
+                                      int(lo), int(hi), int(threads or max_threads()),
+                                      out.ctypes.data_as(p64))
+    if st != 0:
+        raise RuntimeError("oracle failed")
+    return [int(x) for x in out]
+
+
+def affine_exact(constant, linear, threads: int = 0) -> list[int]:
+    """Exact coefficients of per(C + x L) by CRT over oracle residues
+    (bound: coefficients of prod_i (sum_j |c_ij| + x sum_j |l_ij|))."""
+    c = [[int(x) for x in r] for r in constant]
+    l = [[int(x) for x in r] for r in linear]
+    n = len(c)
+    if n == 0:
+        return [1]
+    bound = [1]
+    for i in range(n):
+        a, b = sum(abs(x) for x in c[i]), sum(abs(x) for x in l[i])
+        bound = [(bound[k] if k < len(bound) else 0) * a + (bound[k - 1] * b if k else 0)
+                 for k in range(len(bound) + 1)]
+    target, primes, prod, q = 2 * max(bound) + 1, [], 1, (1 << 31) - 1
+    while prod < target:
+        if _is_prime(q):
+            primes.append(q)
+            prod *= q
+        q -= 2
+    res = [affine_mod_p(c, l, q, threads) for q in primes]
+    out = []
+    for k in range(n + 1):
+        x, m = res[0][k], primes[0]
+        for r, q in zip(res[1:], primes[1:]):
+            x += m * ((r[k] - x) * pow(m, -1, q) % q)
+            m *= q
+        out.append(x - prod if x > prod // 2 else x)
+    return out
 
 
 def reference_modules():

@@ -22,6 +22,11 @@
  *                           ldexp(-(n-1)) at :405), also returning sum |terms|
  *   or_glynn_f64_grad       d per / d a_ij = per(A without row i, column j),
  *                           evaluated by Glynn on every minor (small n only)
+ *   or_affine_mod_p         coefficients of per(C + x L) mod an odd modulus:
+ *                           the fixed-sign Glynn sum with affine row sums and
+ *                           the product of n linear factors per state
+ *                           (perm_polynomial.py:268-329, native engine
+ *                           perm_polynomial_omp.c:434-486, 612-636, 681-779)
  *
  * Parity of this restatement is pinned against the reference's own compiled
  * extensions and golden values in tests/golden (see tests/test_oracle_pins.py).
@@ -414,4 +419,126 @@ void or_glynn_f64_grad(const double *a, int n, int threads, double *grad) {
         double dummy;
         grad[ij] = or_glynn_f64(minor, k, 1, &dummy);
     }
+}
+
+/* Coefficients of per(C + x L) mod odd m (1 < m < 2^63), out[0..n] ascending
+ * degree: 2^(1-n) sum over the 2^(n-1) fixed-sign Gray states of
+ * (prod d) prod_i (c_i(d) + x l_i(d)), with c_i, l_i the signed row sums of
+ * C and L (perm_polynomial.py:268-329).  Contiguous Gray blocks per thread
+ * with closed-form block starts, as or_glynn_mod_p. */
+static void affine_block(const int64_t *c, const int64_t *l, int n, int64_t p,
+                         uint64_t lo, uint64_t hi, int64_t *acc) {
+    int64_t cs[64], ls[64], poly[65], next[65];
+    const uint64_t g0 = lo ^ (lo >> 1);
+    for (int i = 0; i < n; i++) {
+        int64_t a = 0, b = 0;
+        for (int j = 0; j < n; j++) {
+            int neg = j < n - 1 && ((g0 >> j) & 1);
+            a = neg ? sub_mod(a, c[i * n + j], p) : add_mod(a, c[i * n + j], p);
+            b = neg ? sub_mod(b, l[i * n + j], p) : add_mod(b, l[i * n + j], p);
+        }
+        cs[i] = a;
+        ls[i] = b;
+    }
+    int sign_neg = __builtin_popcountll(g0) & 1;
+    uint64_t g = g0;
+    for (uint64_t s = lo; s < hi; s++) {
+        if (s != lo) {
+            const int j = __builtin_ctzll(s);
+            const int sub = !((g >> j) & 1);     /* sign of column j flips to - */
+            g ^= 1ull << j;
+            for (int i = 0; i < n; i++) {
+                const int64_t dc = add_mod(c[i * n + j], c[i * n + j], p);
+                const int64_t dl = add_mod(l[i * n + j], l[i * n + j], p);
+                cs[i] = sub ? sub_mod(cs[i], dc, p) : add_mod(cs[i], dc, p);
+                ls[i] = sub ? sub_mod(ls[i], dl, p) : add_mod(ls[i], dl, p);
+            }
+            sign_neg ^= 1;
+        }
+        int deg = 0;
+        poly[0] = 1 % p;
+        for (int i = 0; i < n; i++) {
+            next[0] = mul_mod(poly[0], cs[i], p);
+            for (int k = 1; k <= deg; k++)
+                next[k] = add_mod(mul_mod(poly[k], cs[i], p), mul_mod(poly[k - 1], ls[i], p), p);
+            next[deg + 1] = mul_mod(poly[deg], ls[i], p);
+            deg++;
+            memcpy(poly, next, (size_t)(deg + 1) * sizeof(int64_t));
+        }
+        for (int k = 0; k <= n; k++)
+            acc[k] = sign_neg ? sub_mod(acc[k], poly[k], p) : add_mod(acc[k], poly[k], p);
+    }
+}
+
+/* Unscaled partial coefficient sums over Gray states [lo, hi) (the CPU
+ * baseline sample of or_affine_mod_p), split over `threads` OpenMP threads. */
+int or_affine_range_mod_p(const int64_t *C, const int64_t *L, int n, int64_t p, uint64_t lo,
+                          uint64_t hi, int threads, int64_t *out) {
+    if (n < 2 || n >= 64 || p < 3 || !(p & 1) || lo >= hi) return -1;
+    int64_t *c = (int64_t *)malloc(sizeof(int64_t) * (size_t)n * n * 2);
+    if (!c) return -1;
+    int64_t *l = c + (size_t)n * n;
+    for (int i = 0; i < n * n; i++) {
+        c[i] = norm_mod(C[i], p);
+        l[i] = norm_mod(L[i], p);
+    }
+    const uint64_t span = hi - lo;
+    int nt = threads > 0 ? threads : 1;
+    if ((uint64_t)nt > span) nt = (int)span;
+    int64_t *accs = (int64_t *)calloc((size_t)nt * 65, sizeof(int64_t));
+    if (!accs) { free(c); return -1; }
+#pragma omp parallel for num_threads(nt) schedule(static)
+    for (int t = 0; t < nt; t++) {
+        const uint64_t b0 = lo + span / nt * t + ((uint64_t)t < span % nt ? t : span % nt);
+        const uint64_t len = span / nt + ((uint64_t)t < span % nt ? 1 : 0);
+        affine_block(c, l, n, p, b0, b0 + len, accs + (size_t)t * 65);
+    }
+    for (int k = 0; k <= n; k++) {
+        int64_t s = 0;
+        for (int t = 0; t < nt; t++) s = add_mod(s, accs[(size_t)t * 65 + k], p);
+        out[k] = s;
+    }
+    free(accs);
+    free(c);
+    return 0;
+}
+
+int or_affine_mod_p(const int64_t *C, const int64_t *L, int n, int64_t p, int threads,
+                    int64_t *out) {
+    if (n < 0 || n >= 64 || p < 3 || !(p & 1)) return -1;
+    if (n == 0) { out[0] = 1 % p; return 0; }
+    int64_t *c = (int64_t *)malloc(sizeof(int64_t) * (size_t)n * n * 2);
+    if (!c) return -1;
+    int64_t *l = c + (size_t)n * n;
+    for (int i = 0; i < n * n; i++) {
+        c[i] = norm_mod(C[i], p);
+        l[i] = norm_mod(L[i], p);
+    }
+    if (n == 1) {
+        out[0] = c[0];
+        out[1] = l[0];
+        free(c);
+        return 0;
+    }
+    const uint64_t states = 1ull << (n - 1);
+    int nt = threads > 0 ? threads : 1;
+    if ((uint64_t)nt > states) nt = (int)states;
+    int64_t *accs = (int64_t *)calloc((size_t)nt * 65, sizeof(int64_t));
+    if (!accs) { free(c); return -1; }
+#pragma omp parallel for num_threads(nt) schedule(static)
+    for (int t = 0; t < nt; t++) {
+        const uint64_t lo = states / nt * t + ((uint64_t)t < states % nt ? t : states % nt);
+        const uint64_t len = states / nt + ((uint64_t)t < states % nt ? 1 : 0);
+        affine_block(c, l, n, p, lo, lo + len, accs + (size_t)t * 65);
+    }
+    const int64_t inv2 = (p >> 1) + 1;
+    const int64_t scale = pow_mod(inv2, (uint64_t)(n - 1), p);
+    for (int k = 0; k <= n; k++) {
+        int64_t s = 0;
+        for (int t = 0; t < nt; t++) s = add_mod(s, accs[(size_t)t * 65 + k], p);
+        out[k] = mul_mod(s, scale, p);
+    }
+    free(accs);
+    free(c);
+    return 0;
 }

@@ -53,6 +53,8 @@ SIGNATURES = {
     "pg_schur_residues_method": ([ctypes.c_int, _c_u64p, _c_u64p, ctypes.c_int, ctypes.c_int,
                                   _c_u64p], ctypes.c_int),
     "pg_necklace_orbit_stats": ([ctypes.c_int, _c_u64p, _c_u64p], ctypes.c_int),
+    "pg_affine_residues": ([_c_i64p, _c_i64p, ctypes.c_int, _c_u64p, ctypes.c_int, _c_u64p],
+                           ctypes.c_int),
     "pg_binary_residues": ([_c_u8p, ctypes.c_int, _c_u64p, ctypes.c_int, _c_u64p], ctypes.c_int),
     "pg_exact_permanent": ([_c_i64p, ctypes.c_int, _c_u32p, ctypes.c_int], ctypes.c_int),
     "pg_exact_supported": ([_c_i64p, ctypes.c_int], ctypes.c_int),
@@ -174,6 +176,20 @@ def necklace_orbit_stats(n: int) -> tuple[int, int]:
         raise ValueError(load().pg_last_error().decode())
     check(st)
     return int(reps.value), int(words.value)
+
+
+def affine_residues(constant, linear, moduli) -> list[list[int]]:
+    """[coefficients of per(C + x L) mod m for m in moduli] (odd m < 2^30,
+    int64 entries, order <= 32)."""
+    c = np.ascontiguousarray(constant, dtype=np.int64)
+    l = np.ascontiguousarray(linear, dtype=np.int64)
+    n = c.shape[0] if c.ndim == 2 else 0
+    mods = np.ascontiguousarray(np.asarray(list(moduli), dtype=np.uint64))
+    out = np.zeros((len(mods), n + 1), dtype=np.uint64)
+    check(load().pg_affine_residues(ptr(c, ctypes.c_int64), ptr(l, ctypes.c_int64), n,
+                                    ptr(mods, ctypes.c_uint64), len(mods),
+                                    ptr(out, ctypes.c_uint64)))
+    return [[int(x) for x in row] for row in out]
 
 
 def binary_residues(matrix: np.ndarray, primes) -> list[int]:

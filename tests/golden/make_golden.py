@@ -42,6 +42,8 @@ def main():
     ap.add_argument("--slow", action="store_true")
     ap.add_argument("--necklace-only", action="store_true",
                     help="regenerate only necklace_stats.json")
+    ap.add_argument("--poly-only", action="store_true",
+                    help="regenerate only poly.json")
     args = ap.parse_args()
 
     ref = Path(args.reference)
@@ -60,6 +62,45 @@ def main():
 
     # ---- necklace quotient statistics (tests/test_schur_cpu_glynn.py:120-130
     #      checks the same counts against Burnside's lemma) -------------------
+    # ---- polynomial permanents (perm_polynomial.py, native engine built by
+    #      oracle/build_ref.sh) ------------------------------------------
+    if not args.necklace_only:
+        import perm_polynomial as pp
+        assert pp.polynomial_backend_capabilities()["native_extension_available"]
+        prng = random.Random(20261203)
+        affine, principal, rook, wrook = [], [], [], []
+        for n in (0, 1, 2, 3, 5, 8, 11, 14, 16):
+            c = [[prng.randint(-9, 9) for _ in range(n)] for _ in range(n)]
+            l = [[prng.randint(-9, 9) for _ in range(n)] for _ in range(n)]
+            mods = [3, 9, 1_000_003, 2_147_483_647, 3_037_000_501, INT64_MAX]
+            affine.append({"constant": c, "linear": l,
+                           "exact": [str(v) for v in pp.affine_permanent(c, l)],
+                           "bounds": [str(v) for v in pp.affine_permanent_bounds(c, l)],
+                           "moduli": mods,
+                           "residues": [list(pp.affine_permanent_mod(c, l, m)) for m in mods]})
+        big = [[prng.randint(-(1 << 50), 1 << 50) for _ in range(6)] for _ in range(6)]
+        lin = [[prng.randint(0, 3) for _ in range(6)] for _ in range(6)]
+        affine.append({"constant": big, "linear": lin,
+                       "exact": [str(v) for v in pp.affine_permanent(big, lin)],
+                       "bounds": [str(v) for v in pp.affine_permanent_bounds(big, lin)],
+                       "moduli": [], "residues": []})
+        for n in (4, 9, 13, 18):
+            a = [[prng.randint(-4, 4) for _ in range(n)] for _ in range(n)]
+            principal.append({"matrix": a,
+                              "exact": [str(v) for v in pp.principal_permanent_polynomial(a)],
+                              "mod_1000003": list(pp.principal_permanent_polynomial_mod(a, 1_000_003))})
+        for n, dens in ((5, 0.5), (10, 0.4), (16, 0.5), (20, 0.3), (22, 0.5)):
+            a = [[int(prng.random() < dens) for _ in range(n)] for _ in range(n)]
+            rook.append({"matrix": a, "rook": [str(v) for v in pp.rook_polynomial(a)]})
+        for n in (4, 8, 12, 15):
+            a = [[prng.randint(0, 7) * (prng.random() < 0.6) for _ in range(n)] for _ in range(n)]
+            wrook.append({"matrix": a, "rook": [str(v) for v in pp.weighted_rook_polynomial(a)]})
+        dump("poly.json", {"source": "perm_polynomial (native engine perm_polynomial_omp.c)",
+                           "affine": affine, "principal": principal, "rook": rook,
+                           "weighted_rook": wrook})
+    if args.poly_only:
+        return
+
     stats = {}
     for n in (3, 5, 7, 11, 13, 17, 19, 23, 29, 31):
         reps, words = perm_c_ext.schur_necklace_orbit_stats(n)

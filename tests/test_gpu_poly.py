@@ -1,0 +1,86 @@
+"""GPU parity of the affine-polynomial engine (pg_affine_residues) and the
+polynomial API built on it: coefficient residues bit-exact against the
+oracle, exact vectors against the reference's perm_polynomial results, and
+full-size identities."""
+
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+MODULI = [3, 9, 15, 1_000_003, 536_870_909, 1_073_741_789]   # odd, some composite
+
+
+@pytest.mark.parametrize("n", list(range(2, 21)))
+def test_residues_match_oracle(lib, n):
+    rng = np.random.default_rng(900 + n)
+    c = rng.integers(-(1 << 40), 1 << 40, (n, n))
+    l = rng.integers(-9, 10, (n, n))
+    got = lib.affine_residues(c, l, MODULI)
+    for m, row in zip(MODULI, got):
+        assert row == oracle.affine_mod_p(c, l, m), (n, m)
+
+
+def test_exact_vectors_match_reference():
+    import permgpu
+    data = golden("poly.json")
+    for c in data["affine"]:
+        assert permgpu.affine_permanent(c["constant"], c["linear"]) == \
+            tuple(int(v) for v in c["exact"])
+        for m, want in zip(c["moduli"], c["residues"]):
+            assert permgpu.affine_permanent_mod(c["constant"], c["linear"], m) == tuple(want)
+    for c in data["principal"]:
+        assert permgpu.principal_permanent_polynomial(c["matrix"]) == \
+            tuple(int(v) for v in c["exact"])
+        assert permgpu.principal_permanent_polynomial_mod(c["matrix"], 1_000_003) == \
+            tuple(c["mod_1000003"])
+    for c in data["rook"]:
+        assert permgpu.rook_polynomial(c["matrix"]) == tuple(int(v) for v in c["rook"])
+    for c in data["weighted_rook"]:
+        assert permgpu.weighted_rook_polynomial(c["matrix"]) == tuple(int(v) for v in c["rook"])
+
+
+@pytest.mark.parametrize("n", [6, 17, 24])
+def test_rook_polynomial_of_all_ones(n):
+    import permgpu
+    want = tuple(math.comb(n, k) ** 2 * math.factorial(k) for k in range(n + 1))
+    assert permgpu.rook_polynomial([[1] * n for _ in range(n)]) == want
+
+
+def test_full_size_rook_identities():
+    # 28x28 Bernoulli(0.5): r_1 = number of ones, r_n = per(A) from the
+    # exact engine, sum_k r_k (n-k)! = per(J + A) ... checked through the
+    # top and bottom coefficients
+    import permgpu
+    a = (np.random.default_rng(28).random((28, 28)) < 0.5).astype(int)
+    r = permgpu.rook_polynomial(a.tolist())
+    assert r[0] == 1 and r[1] == int(a.sum())
+    assert r[28] == permgpu.binary_permanent(a.tolist())
+
+
+def test_principal_polynomial_identities():
+    import permgpu
+    n = 22
+    # per(I + x I) = (1 + x)^n
+    eye = [[int(i == j) for j in range(n)] for i in range(n)]
+    assert permgpu.principal_permanent_polynomial(eye) == \
+        tuple(math.comb(n, k) for k in range(n + 1))
+    # top coefficient of per(I + x A) is per(A)
+    a = np.random.default_rng(22).integers(-3, 4, (n, n))
+    top = permgpu.principal_permanent_polynomial(a.tolist())[-1]
+    assert top == permgpu.matrix_permanent(a.tolist())
+
+
+def test_wide_modulus_goes_through_the_exact_vector():
+    import permgpu
+    rng = np.random.default_rng(17)
+    c = rng.integers(-5, 6, (12, 12)).tolist()
+    l = rng.integers(-5, 6, (12, 12)).tolist()
+    exact = permgpu.affine_permanent(c, l)
+    for m in (3_037_000_501, (1 << 63) - 1):
+        assert permgpu.affine_permanent_mod(c, l, m) == tuple(v % m for v in exact)

@@ -132,3 +132,20 @@ def test_float_gradient_oracle_matches_reference_minors():
     assert np.array_equal(g, want)
     v, _ = oracle.glynn_f64(a, 8)
     assert v == float(int(c["permanent"]))
+
+
+def test_affine_oracle_matches_reference_polynomial_engine():
+    # oracle/oracle_perm.c or_affine_mod_p vs perm_polynomial (native engine)
+    data = golden("poly.json")
+    for c in data["affine"]:
+        n = len(c["constant"])
+        for m, want in zip(c["moduli"], c["residues"]):
+            if n < 2:
+                continue
+            assert oracle.affine_mod_p(c["constant"], c["linear"], m) == want
+        if n >= 2 and max(abs(v) for row in c["constant"] for v in row) < (1 << 40):
+            assert oracle.affine_exact(c["constant"], c["linear"]) == [int(v) for v in c["exact"]]
+    for c in data["principal"]:
+        n = len(c["matrix"])
+        eye = [[int(i == j) for j in range(n)] for i in range(n)]
+        assert oracle.affine_mod_p(eye, c["matrix"], 1_000_003) == c["mod_1000003"]
