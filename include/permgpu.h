@@ -116,6 +116,24 @@ int pg_affine_residues(const int64_t *C, const int64_t *L, int n,
                        const uint64_t *moduli, int k, uint64_t *out);
 
 /*
+ * Permanent modulo 3 (*out in {0, 1, 2}) by Ryser's formula over F_3 with
+ * bit-sliced row sums, 0 <= n < 64, any int64 entries.  Replaces
+ * permanent_mod3_matrix (perm_mod3_cuda.cu:300-349) and the OpenMP
+ * perm_mod3_omp.permanent_mod3 behind perm_mod3.permanent_mod3_fast
+ * (perm_mod3.py:355-383).
+ */
+int pg_permanent_mod3(const int64_t *A, int n, int *out);
+
+/*
+ * The same from the F_3 column encodings: bit i of col_mags[j] is set when
+ * a_ij != 0 (mod 3), bit i of col_sgns[j] when a_ij == 2 (mod 3); sign bits
+ * must lie inside the magnitude bits.  Replaces permanent_mod3_cuda
+ * (perm_mod3_cuda.cu:164-296), encodings as perm_mod3.encode_matrix_f3.
+ */
+int pg_permanent_mod3_cols(const uint64_t *col_mags, const uint64_t *col_sgns,
+                           int n, int *out);
+
+/*
  * Binary residues: out[t] = per(A) mod primes[t] for a 0/1 matrix.
  * Contract of perm_binary_ext.binary_permanent_mod_p (perm_binary_omp.c:
  * 386-519) and binary_permanent_modp_cuda (perm_binary_cuda.cu:471-482):

@@ -1,9 +1,9 @@
 #!/usr/bin/env bash
 # Compile the reference's own OpenMP extensions (perm_c_omp.c,
-# perm_binary_omp.c and perm_polynomial_omp.c) from the reference checkout
-# into oracle/_ref/.  These are CPython extension modules used only as the CPU
-# checker, the golden-vector generator and the CPU baseline; no reference
-# source is copied into this repository.
+# perm_binary_omp.c, perm_polynomial_omp.c and perm_mod3_omp.c) from the
+# reference checkout into oracle/_ref/.  These are CPython extension modules
+# used only as the CPU checker, the golden-vector generator and the CPU
+# baseline; no reference source is copied into this repository.
 #
 # usage: oracle/build_ref.sh [REFERENCE_DIR]   (default /root/reference)
 set -euo pipefail
@@ -16,10 +16,13 @@ if [ ! -f "$REF/perm_c_omp.c" ]; then
 fi
 mkdir -p "$OUT"
 PYINC="$(python3 -c 'import sysconfig; print(sysconfig.get_paths()["include"])')"
+NPINC="$(python3 -c 'import numpy; print(numpy.get_include())')"
 SUFFIX="$(python3 -c 'import sysconfig; print(sysconfig.get_config_var("EXT_SUFFIX"))')"
 gcc -O3 -fopenmp -fPIC -shared -I"$PYINC" "$REF/perm_c_omp.c" -o "$OUT/perm_c_ext$SUFFIX" &
 gcc -O3 -fopenmp -fPIC -shared -I"$PYINC" "$REF/perm_binary_omp.c" -o "$OUT/perm_binary_ext$SUFFIX" &
 gcc -O3 -std=c11 -fopenmp -fPIC -shared -I"$PYINC" "$REF/perm_polynomial_omp.c" \
     -o "$OUT/perm_polynomial_ext$SUFFIX" &
+gcc -O3 -fopenmp -fPIC -shared -I"$PYINC" -I"$NPINC" "$REF/perm_mod3_omp.c" \
+    -o "$OUT/perm_mod3_omp$SUFFIX" &
 wait
-echo "built $OUT/perm_c_ext$SUFFIX $OUT/perm_binary_ext$SUFFIX $OUT/perm_polynomial_ext$SUFFIX"
+echo "built the reference extensions into $OUT"

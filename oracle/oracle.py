@@ -44,8 +44,7 @@ def build(force: bool = False) -> Path:
 def load():
     global _lib
     if _lib is None:
-        if not LIB.exists():
-            build()
+        build()      # no-op unless the library is missing or older than its source
         lib = ctypes.CDLL(str(LIB))
         i64p = ctypes.POINTER(ctypes.c_int64)
         f64p = ctypes.POINTER(ctypes.c_double)
@@ -71,6 +70,11 @@ def load():
         lib.or_glynn_c64.restype = None
         lib.or_max_threads.argtypes = []
         lib.or_max_threads.restype = ctypes.c_int
+        lib.or_mod3_range.argtypes = [i64p, ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64,
+                                      ctypes.c_int]
+        lib.or_mod3_range.restype = ctypes.c_int
+        lib.or_permanent_mod3.argtypes = [i64p, ctypes.c_int, ctypes.c_int]
+        lib.or_permanent_mod3.restype = ctypes.c_int
         lib.or_affine_mod_p.argtypes = [i64p, i64p, ctypes.c_int, ctypes.c_int64, ctypes.c_int, i64p]
         lib.or_affine_mod_p.restype = ctypes.c_int
         lib.or_affine_range_mod_p.argtypes = [i64p, i64p, ctypes.c_int, ctypes.c_int64,
@@ -236,6 +240,21 @@ def affine_mod_p(constant, linear, p: int, threads: int = 0) -> list[int]:
     if st != 0:
         raise RuntimeError("oracle failed")
     return [int(x) for x in out]
+
+
+def permanent_mod3(matrix, threads: int = 0) -> int:
+    """per(A) mod 3 by the bit-sliced F_3 Ryser walk (perm_mod3_omp.c)."""
+    a = _i64(matrix)
+    n = a.shape[0] if a.ndim == 2 else 0
+    return int(load().or_permanent_mod3(a.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), n,
+                                        int(threads or max_threads())))
+
+
+def mod3_range(matrix, lo: int, hi: int, threads: int = 0) -> int:
+    """Partial bit-sliced Ryser sum over subsets [lo, hi), as a count mod 3."""
+    a = _i64(matrix)
+    return int(load().or_mod3_range(a.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                                    a.shape[0], int(lo), int(hi), int(threads or max_threads())))
 
 
 def affine_range_mod_p(constant, linear, p: int, lo: int, hi: int, threads: int = 0) -> list[int]:

@@ -22,6 +22,9 @@
  *                           ldexp(-(n-1)) at :405), also returning sum |terms|
  *   or_glynn_f64_grad       d per / d a_ij = per(A without row i, column j),
  *                           evaluated by Glynn on every minor (small n only)
+ *   or_mod3_range           Ryser mod 3 with bit-sliced F_3 row sums over a
+ *                           range of the 2^n Gray-ordered subsets
+ *                           (perm_mod3_omp.c:54-160, perm_mod3.py:143-228)
  *   or_affine_mod_p         coefficients of per(C + x L) mod an odd modulus:
  *                           the fixed-sign Glynn sum with affine row sums and
  *                           the product of n linear factors per state
@@ -468,6 +471,66 @@ static void affine_block(const int64_t *c, const int64_t *l, int n, int64_t p,
         for (int k = 0; k <= n; k++)
             acc[k] = sign_neg ? sub_mod(acc[k], poly[k], p) : add_mod(acc[k], poly[k], p);
     }
+}
+
+/* Sum over Gray-ordered subsets [lo, hi) of (-1)^|S| prod_i sum_{j in S} a_ij
+ * over F_3, as a count mod 3 (entries already reduced to {0,1,2}); the full
+ * range times (-1)^n is per(A) mod 3.  Row sums are two bit words
+ * (magnitude, sign) updated per column toggle. */
+int or_mod3_range(const int64_t *A, int n, uint64_t lo, uint64_t hi, int threads) {
+    if (n < 1 || n >= 64 || lo >= hi) return 0;
+    uint64_t cm[64], cs[64];
+    for (int j = 0; j < n; j++) {
+        cm[j] = cs[j] = 0;
+        for (int i = 0; i < n; i++) {
+            const int v = (int)norm_mod(A[i * n + j], 3);
+            if (v) cm[j] |= 1ull << i;
+            if (v == 2) cs[j] |= 1ull << i;
+        }
+    }
+    const uint64_t mask = n == 64 ? ~0ull : ((1ull << n) - 1);
+    const uint64_t span = hi - lo;
+    int nt = threads > 0 ? threads : 1;
+    if ((uint64_t)nt > span) nt = (int)span;
+    uint64_t total = 0;
+#pragma omp parallel for num_threads(nt) schedule(static) reduction(+ : total)
+    for (int t = 0; t < nt; t++) {
+        const uint64_t b0 = lo + span / nt * t + ((uint64_t)t < span % nt ? t : span % nt);
+        const uint64_t b1 = b0 + span / nt + ((uint64_t)t < span % nt ? 1 : 0);
+        uint64_t m = 0, s = 0, cnt = 0;
+        const uint64_t g0 = b0 ^ (b0 >> 1);
+        for (int j = 0; j < n; j++)
+            if ((g0 >> j) & 1) {
+                const uint64_t u = m ^ s ^ cs[j], mo = (cm[j] & u) | (m ^ cm[j]);
+                s = (cm[j] & u) ^ s;
+                m = mo;
+            }
+        for (uint64_t i = b0; i < b1; i++) {
+            if (i != b0) {
+                const int j = __builtin_ctzll(i);
+                if (((i >> (j + 1)) & 1) == 0) {          /* column j enters S */
+                    const uint64_t u = m ^ s ^ cs[j], mo = (cm[j] & u) | (m ^ cm[j]);
+                    s = (cm[j] & u) ^ s;
+                    m = mo;
+                } else {                                  /* column j leaves S */
+                    const uint64_t u = s ^ cs[j], mo = (m & u) | (m ^ cm[j]);
+                    s = (m & u) ^ (cm[j] ^ cs[j]);
+                    m = mo;
+                }
+            }
+            if ((m & mask) == mask)
+                cnt += 1 + ((__builtin_popcountll(s & mask) ^ (int)(i & 1)) & 1);
+        }
+        total += cnt % 3;
+    }
+    return (int)(total % 3);
+}
+
+int or_permanent_mod3(const int64_t *A, int n, int threads) {
+    if (n == 0) return 1;
+    if (n == 1) return (int)norm_mod(A[0], 3);
+    const int t = or_mod3_range(A, n, 0, 1ull << n, threads);
+    return (n & 1) ? (3 - t) % 3 : t;
 }
 
 /* Unscaled partial coefficient sums over Gray states [lo, hi) (the CPU

@@ -53,6 +53,8 @@ SIGNATURES = {
     "pg_schur_residues_method": ([ctypes.c_int, _c_u64p, _c_u64p, ctypes.c_int, ctypes.c_int,
                                   _c_u64p], ctypes.c_int),
     "pg_necklace_orbit_stats": ([ctypes.c_int, _c_u64p, _c_u64p], ctypes.c_int),
+    "pg_permanent_mod3": ([_c_i64p, ctypes.c_int, _c_intp], ctypes.c_int),
+    "pg_permanent_mod3_cols": ([_c_u64p, _c_u64p, ctypes.c_int, _c_intp], ctypes.c_int),
     "pg_affine_residues": ([_c_i64p, _c_i64p, ctypes.c_int, _c_u64p, ctypes.c_int, _c_u64p],
                            ctypes.c_int),
     "pg_binary_residues": ([_c_u8p, ctypes.c_int, _c_u64p, ctypes.c_int, _c_u64p], ctypes.c_int),
@@ -176,6 +178,24 @@ def necklace_orbit_stats(n: int) -> tuple[int, int]:
         raise ValueError(load().pg_last_error().decode())
     check(st)
     return int(reps.value), int(words.value)
+
+
+def permanent_mod3(matrix) -> int:
+    """per(A) mod 3 for an int64 matrix of order < 64."""
+    a = np.ascontiguousarray(matrix, dtype=np.int64)
+    n = a.shape[0] if a.ndim == 2 else 0
+    out = ctypes.c_int()
+    check(load().pg_permanent_mod3(ptr(a, ctypes.c_int64), n, ctypes.byref(out)))
+    return int(out.value)
+
+
+def permanent_mod3_cols(col_mags, col_sgns, n: int) -> int:
+    m = np.ascontiguousarray(np.asarray(col_mags, dtype=np.uint64))
+    s = np.ascontiguousarray(np.asarray(col_sgns, dtype=np.uint64))
+    out = ctypes.c_int()
+    check(load().pg_permanent_mod3_cols(ptr(m, ctypes.c_uint64), ptr(s, ctypes.c_uint64),
+                                        int(n), ctypes.byref(out)))
+    return int(out.value)
 
 
 def affine_residues(constant, linear, moduli) -> list[list[int]]:

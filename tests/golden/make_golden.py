@@ -98,6 +98,17 @@ def main():
         dump("poly.json", {"source": "perm_polynomial (native engine perm_polynomial_omp.c)",
                            "affine": affine, "principal": principal, "rook": rook,
                            "weighted_rook": wrook})
+        # ---- permanents mod 3 (perm_mod3.permanent_mod3_fast, OpenMP ext)
+        import perm_mod3
+        assert perm_mod3.HAS_MOD3_OMP
+        mrng = np.random.default_rng(20261204)
+        mod3 = []
+        for n in (2, 3, 4, 7, 12, 17, 21, 26, 30, 32, 33):
+            for low, high in ((-100, 100), (0, 2)):
+                a = mrng.integers(low, high, (n, n)).astype(np.int64)
+                mod3.append({"matrix": a.tolist(), "mod3": perm_mod3.permanent_mod3_fast(a)})
+        dump("mod3.json", {"source": "perm_mod3.permanent_mod3_fast (perm_mod3_omp.c)",
+                           "cases": mod3})
     if args.poly_only:
         return
 
