@@ -606,8 +606,8 @@ def run_gpu_mod3(args, world, rank, local):
     import torch
     from permgpu import _lib, mod3
     torch.cuda.set_device(local)
-    n = 40
-    a = np.random.default_rng(40 + rank).integers(0, 3, (n, n)).astype(np.int64)
+    n = args.mod3_order
+    a = np.random.default_rng(n + rank).integers(0, 3, (n, n)).astype(np.int64)
     states = 1 << n
     for _ in range(args.warmup):
         got = mod3.permanent_mod3_fast(a)
@@ -645,12 +645,12 @@ def run_gpu_mod3(args, world, rank, local):
         # per subset: one 64-bit column update (3 three-input bitwise ops on
         # two words), the full-magnitude test and a popcount
         print(json.dumps({
-            "metric": "Ryser subsets/s (perm mod 3, 40x40)", "value": world * states / step_s,
+            "metric": f"Ryser subsets/s (perm mod 3, {n}x{n})", "value": world * states / step_s,
             "unit": "subsets/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * step_s, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "F_3 bit-sliced (u64 words)", "data": "synthetic",
-            "config": {"workload": "mod3_40: 40x40 matrix, entries U{0,1,2}, numpy "
-                                   "default_rng(40)", "subsets": states},
+            "config": {"workload": f"mod3_40: {n}x{n} matrix, entries U{{0,1,2}}, numpy "
+                                   f"default_rng({n})", "subsets": states},
             "time_to_result_s": step_s, "result": got, "cpu_baseline": cpu,
             "e2e": {"value": world * states / step_s, "unit": "subsets/s",
                     "h2d_bytes_per_step": 2 * 8 * n, "d2h_bytes_per_step": 16,
@@ -779,6 +779,8 @@ def main():
                     help="float28: matrices per step (256 is the workload; smaller for profiling)")
     ap.add_argument("--order", type=int, default=41,
                     help="schur41: prime Schur order (41 is the workload; 37 for profiling)")
+    ap.add_argument("--mod3-order", type=int, default=40,
+                    help="mod3_40: matrix order (40 is the workload; smaller for profiling)")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":

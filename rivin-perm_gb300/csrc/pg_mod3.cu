@@ -109,9 +109,12 @@ __global__ void __launch_bounds__(256) mod3_kernel(Mod3Args a) {
                         if (add) f3_add(m, s, cmj, csj);
                         else f3_sub(m, s, cmj, csj);
                     }
-                    // subset sign (-1)^|S| = (-1)^(popcount(gray(i))) = (-1)^(i & 1) = (-1)^r
-                    const int neg = f3_parity(s & mask) ^ (r & 1);
-                    count += ((m & mask) == mask) ? (unsigned long long)(1 + neg) : 0ull;
+                    // Bits above row n stay 0 in both words, so "every row sum
+                    // nonzero" is m == mask.  That is rare (about (2/3)^n for
+                    // random entries), so the sign work sits behind a branch
+                    // that is almost never taken.
+                    // Subset sign (-1)^|S| = (-1)^popcount(gray(i)) = (-1)^r.
+                    if (m == mask) count += (unsigned long long)(1 + (f3_parity(s) ^ (r & 1)));
                 }
             }
         }
