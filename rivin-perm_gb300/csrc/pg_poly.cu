@@ -49,23 +49,38 @@ __device__ __forceinline__ uint32_t poly_redc2(uint32_t a, uint32_t c, uint32_t 
     return (uint32_t)(((uint64_t)m * p + t) >> 32);
 }
 
+// From order 20 on the n+1 coefficient accumulators move from registers to
+// shared memory (one word per coefficient and thread, thread-minor so a warp
+// touches 32 consecutive banks) and blocks shrink to 128 threads: the row
+// sums and the coefficient vector alone fill most of the register file, and
+// fewer registers per thread let three or more blocks share an SM.
+__host__ __device__ constexpr bool poly_acc_in_smem(int N) { return N >= 20; }
+__host__ __device__ constexpr int poly_block(int N) { return poly_acc_in_smem(N) ? 128 : 256; }
+
 template <int N>
-__global__ void __launch_bounds__(256) affine_m32_kernel(PolyArgs a) {
+__global__ void __launch_bounds__(poly_block(N)) affine_m32_kernel(PolyArgs a) {
     constexpr int NP = (N + 3) & ~3;
     constexpr int NCOL = N - 1;
+    constexpr bool ACC_SM = poly_acc_in_smem(N);
+    constexpr int BT = poly_block(N);
     extern __shared__ uint4 psm[];
     uint32_t *tab = reinterpret_cast<uint32_t *>(psm);
+    uint32_t *accs = tab + NCOL * 4 * NP;   // [N+1][BT] when ACC_SM
     const int k = blockIdx.y;
     {
         const uint4 *g = reinterpret_cast<const uint4 *>(a.tabs + (size_t)k * NCOL * 4 * NP);
         for (int i = threadIdx.x; i < NCOL * 4 * NP / 4; i += blockDim.x) psm[i] = g[i];
     }
-    __syncthreads();
     const uint32_t p = a.moduli[k], pinv = a.pinvs[k];
 
-    uint32_t acc[N + 1];
+    uint32_t acc[ACC_SM ? 1 : N + 1];
+    if constexpr (ACC_SM) {
+        for (int d = 0; d <= N; d++) accs[d * BT + threadIdx.x] = 0;
+    } else {
 #pragma unroll
-    for (int d = 0; d <= N; d++) acc[d] = 0;
+        for (int d = 0; d <= N; d++) acc[d] = 0;
+    }
+    __syncthreads();
     bool aborted = false;
 
     const uint64_t T = (uint64_t)gridDim.x * blockDim.x;
@@ -135,21 +150,28 @@ __global__ void __launch_bounds__(256) affine_m32_kernel(PolyArgs a) {
 #pragma unroll
             for (int d = 0; d <= N; d++) {
                 const uint32_t v = __viaddmin_u32(P[d], 0u - p, P[d]);   // < p
-                acc[d] = m32_addmod(acc[d], neg ? 0u - v : v - p, p);
+                if constexpr (ACC_SM) {
+                    uint32_t &x = accs[d * BT + threadIdx.x];
+                    x = m32_addmod(x, neg ? 0u - v : v - p, p);
+                } else {
+                    acc[d] = m32_addmod(acc[d], neg ? 0u - v : v - p, p);
+                }
             }
         }
     }
 
     // block reduction per coefficient; residues < 2^30, so 64-bit sums over
     // the whole grid cannot overflow
-    __shared__ unsigned long long red[8][N + 1];
+    __shared__ unsigned long long red[BT / 32][N + 1];
     __shared__ int any_abort;
     if (threadIdx.x == 0) any_abort = 0;
     __syncthreads();
     if (aborted) any_abort = 1;
 #pragma unroll
     for (int d = 0; d <= N; d++) {
-        unsigned long long v = acc[d];
+        unsigned long long v;
+        if constexpr (ACC_SM) v = accs[d * BT + threadIdx.x];
+        else v = acc[d];
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
         if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][d] = v;
@@ -166,21 +188,23 @@ __global__ void __launch_bounds__(256) affine_m32_kernel(PolyArgs a) {
 template <int N>
 static cudaError_t launch_affine_n(const PolyArgs &args, int k, int sm_count, cudaStream_t s) {
     constexpr int NP = (N + 3) & ~3;
-    const size_t smem = (size_t)(N - 1) * 4 * NP * 4;
+    constexpr int BT = poly_block(N);
+    const size_t smem = (size_t)(N - 1) * 4 * NP * 4 +
+                        (poly_acc_in_smem(N) ? (size_t)(N + 1) * BT * 4 : 0);
     cudaError_t e = cudaFuncSetAttribute(affine_m32_kernel<N>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, affine_m32_kernel<N>, 256, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, affine_m32_kernel<N>, BT, smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) per_sm = 1;
     // one resident wave shared by the k moduli, no more blocks than chunks
     uint64_t bpm = ((uint64_t)per_sm * sm_count + k - 1) / k;
-    const uint64_t max_blocks = (args.chunks + 255) / 256;
+    const uint64_t max_blocks = (args.chunks + BT - 1) / BT;
     if (bpm > max_blocks) bpm = max_blocks;
     if (bpm < 1) bpm = 1;
     dim3 grid((unsigned)bpm, (unsigned)k);
-    affine_m32_kernel<N><<<grid, 256, smem, s>>>(args);
+    affine_m32_kernel<N><<<grid, BT, smem, s>>>(args);
     return cudaGetLastError();
 }
 
