@@ -218,6 +218,19 @@ int pg_batch_plan_result(pg_batch_plan *plan, void *stream, uint32_t *out,
 int pg_batch_plan_info(const pg_batch_plan *plan, uint32_t *tasks,
                        int *blocks, uint64_t *kernel_states, int *external);
 void pg_batch_plan_destroy(pg_batch_plan *plan);
+/*
+ * Residues of many matrices, each modulo its own moduli:
+ *   out[moduli_offsets[m] + t] = per(A_m) mod moduli[moduli_offsets[m] + t]
+ * for t < moduli_offsets[m+1] - moduli_offsets[m]; A_m is the row-major
+ * orders[m]^2 block at A + offsets[m].  Matrices the exact engine accepts
+ * run in one batched exact launch (results reduced on the host); the others
+ * take pg_residues with all their moduli in one launch.  Replaces the
+ * per-matrix, per-prime loop over permanent_mod_p (perm.py:1172-1197).
+ */
+int pg_batch_residues(const int64_t *A, const int64_t *offsets,
+                      const int32_t *orders, int count,
+                      const uint64_t *moduli, const int32_t *moduli_offsets,
+                      uint64_t *out);
 int pg_batch_exact(const int64_t *A, const int64_t *offsets,
                    const int32_t *orders, int count, uint32_t *out, int limbs);
 
@@ -236,6 +249,17 @@ int pg_batch_exact(const int64_t *A, const int64_t *offsets,
 int pg_glynn_f64_dev(const double *A, int batch, int n, double *per,
                      double *grad, double *abs_sum, double *grad_abs,
                      void *stream);
+
+/*
+ * pg_glynn_f64_dev with host pointers: A [batch][n][n] f64 in, per[batch],
+ * grad [batch][n][n] (NULL: forward only) and abs_sum[batch] (nullable)
+ * out; 0 <= n <= 32.  Device buffers for the call are allocated and freed
+ * inside, so plain ctypes callers need no device memory of their own.
+ * Replaces permanent_parallel_real (perm_parallel_cuda.cu:343-414) for a
+ * whole batch, with the gradient.
+ */
+int pg_glynn_f64_fwd_bwd(const double *A, int batch, int n, double *per,
+                         double *grad, double *abs_sum);
 
 /*
  * Complex FP64 Glynn permanent (forward) for a batch of complex matrices

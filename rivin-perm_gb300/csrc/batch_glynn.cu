@@ -465,4 +465,84 @@ int pg_batch_exact(const int64_t *A, const int64_t *offsets, const int32_t *orde
     return st;
 }
 
+// Residues of many matrices, each modulo its own list of moduli.  Matrices
+// the exact engine accepts go through one batched exact launch and their
+// exact values are reduced on the host; the others (entries too large for
+// exact int32 row sums) take pg_residues, all of a matrix's moduli in one
+// launch.
+int pg_batch_residues(const int64_t *A, const int64_t *offsets, const int32_t *orders,
+                      int count, const uint64_t *moduli, const int32_t *moduli_offsets,
+                      uint64_t *out) {
+    using namespace pg;
+    if (count < 0) return fail(PG_EINVAL, "count must be non-negative");
+    if (count == 0) return PG_OK;
+    if (!A || !offsets || !orders || !moduli || !moduli_offsets || !out)
+        return fail(PG_EINVAL, "null argument");
+    for (int m = 0; m < count; m++) {
+        if (orders[m] < 0 || orders[m] >= 64) return fail(PG_ERANGE, "orders must be < 64");
+        if (moduli_offsets[m + 1] < moduli_offsets[m]) return fail(PG_EINVAL, "moduli offsets");
+        for (int t = moduli_offsets[m]; t < moduli_offsets[m + 1]; t++)
+            if (moduli[t] == 0 || moduli[t] >= (1ull << 63))
+                return fail(PG_ERANGE, "moduli must satisfy 1 <= m < 2^63");
+    }
+    std::vector<int> exact_ids;
+    std::vector<int64_t> packed, poff;
+    std::vector<int32_t> pord;
+    int limbs = 2;
+    for (int m = 0; m < count; m++) {
+        const int n = orders[m];
+        const int64_t *a = A + offsets[m];
+        if (n < 2 || !pg_exact_supported(a, n)) continue;
+        double bits = 2.0;   // sign and rounding margin
+        for (int i = 0; i < n; i++) {
+            double b = 0;
+            for (int j = 0; j < n; j++) b += std::fabs((double)a[(size_t)i * n + j]);
+            bits += std::log2(std::max(1.0, b));
+        }
+        limbs = std::max(limbs, (int)std::ceil(bits / 32.0) + 1);
+        exact_ids.push_back(m);
+        poff.push_back((int64_t)packed.size());
+        pord.push_back(n);
+        packed.insert(packed.end(), a, a + (size_t)n * n);
+    }
+    std::vector<uint32_t> words((size_t)exact_ids.size() * limbs);
+    if (!exact_ids.empty()) {
+        const int st = pg_batch_exact(packed.data(), poff.data(), pord.data(),
+                                      (int)exact_ids.size(), words.data(), limbs);
+        if (st != PG_OK) return st;
+    }
+    std::vector<char> done(count, 0);
+    for (size_t e = 0; e < exact_ids.size(); e++) {
+        const int m = exact_ids[e];
+        const uint32_t *w = words.data() + e * limbs;
+        const bool negative = (w[limbs - 1] >> 31) != 0;
+        for (int t = moduli_offsets[m]; t < moduli_offsets[m + 1]; t++) {
+            const uint64_t p = moduli[t];
+            // magnitude of the two's-complement value, Horner from the top limb
+            uint64_t r = 0;
+            uint32_t borrow = 1;
+            std::vector<uint32_t> mag(w, w + limbs);
+            if (negative) {
+                for (int i = 0; i < limbs; i++) {   // -x = ~x + 1
+                    const uint64_t v = (uint64_t)(uint32_t)~mag[i] + borrow;
+                    mag[i] = (uint32_t)v;
+                    borrow = (uint32_t)(v >> 32);
+                }
+            }
+            for (int i = limbs - 1; i >= 0; i--)
+                r = (uint64_t)((((unsigned __int128)r << 32) + mag[i]) % p);
+            out[t] = negative && r ? p - r : r;
+        }
+        done[m] = 1;
+    }
+    for (int m = 0; m < count; m++) {
+        if (done[m] || moduli_offsets[m + 1] == moduli_offsets[m]) continue;
+        const int st = pg_residues(A + offsets[m], orders[m], moduli + moduli_offsets[m],
+                                   moduli_offsets[m + 1] - moduli_offsets[m],
+                                   out + moduli_offsets[m]);
+        if (st != PG_OK) return st;
+    }
+    return PG_OK;
+}
+
 }  // extern "C"

@@ -553,3 +553,48 @@ extern "C" int pg_glynn_c64_dev(const double *Are, const double *Aim, int batch,
     if (hstatus) return fail(PG_EABORT, "complex FP64 launch aborted by pg_abort()");
     return PG_OK;
 }
+
+// Host-pointer form of pg_glynn_f64_dev for callers without device memory of
+// their own (ctypes users, other languages' FFIs): device buffers for the
+// call are allocated here (the library's workspace is the kernel's own
+// scratch), the results are copied back and the buffers freed.
+extern "C" int pg_glynn_f64_fwd_bwd(const double *A, int batch, int n, double *per,
+                                    double *grad, double *abs_sum) {
+    using namespace pg;
+    if (batch < 0 || n < 0 || n > 32) return fail(PG_ERANGE, "FP64 engine supports 0 <= n <= 32");
+    if (batch == 0) return PG_OK;
+    if (!per || (n > 0 && !A)) return fail(PG_EINVAL, "null argument");
+    if (n <= 1) {
+        for (int b = 0; b < batch; b++) {
+            per[b] = n == 0 ? 1.0 : A[b];
+            if (grad && n == 1) grad[b] = 1.0;
+            if (abs_sum) abs_sum[b] = n == 0 ? 1.0 : std::fabs(A[b]);
+        }
+        return PG_OK;
+    }
+    DeviceInfo dev;
+    int st = device_info(&dev);
+    if (st != PG_OK) return st;
+    const size_t na = (size_t)batch * n * n;
+    const size_t bytes = (na + (grad ? na : 0) + 2 * (size_t)batch) * sizeof(double);
+    double *d = nullptr;
+    PG_CUDA(cudaMalloc(&d, bytes));
+    double *dA = d, *dgrad = grad ? d + na : nullptr;
+    double *dper = d + na + (grad ? na : 0), *dabs = dper + batch;
+    cudaError_t e = cudaMemcpy(dA, A, na * sizeof(double), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(d);
+        return cuda_fail(e, "cudaMemcpy(A)");
+    }
+    st = pg_glynn_f64_dev(dA, batch, n, dper, dgrad, dabs, nullptr, nullptr);
+    if (st == PG_OK) {
+        e = cudaMemcpy(per, dper, (size_t)batch * sizeof(double), cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess && grad)
+            e = cudaMemcpy(grad, dgrad, na * sizeof(double), cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess && abs_sum)
+            e = cudaMemcpy(abs_sum, dabs, (size_t)batch * sizeof(double), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) st = cuda_fail(e, "cudaMemcpy(results)");
+    }
+    cudaFree(d);
+    return st;
+}

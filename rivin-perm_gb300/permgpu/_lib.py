@@ -53,6 +53,10 @@ SIGNATURES = {
     "pg_schur_residues_method": ([ctypes.c_int, _c_u64p, _c_u64p, ctypes.c_int, ctypes.c_int,
                                   _c_u64p], ctypes.c_int),
     "pg_necklace_orbit_stats": ([ctypes.c_int, _c_u64p, _c_u64p], ctypes.c_int),
+    "pg_glynn_f64_fwd_bwd": ([_c_f64p, ctypes.c_int, ctypes.c_int, _c_f64p, _c_f64p, _c_f64p],
+                             ctypes.c_int),
+    "pg_batch_residues": ([_c_i64p, _c_i64p, _c_i32p, ctypes.c_int, _c_u64p, _c_i32p, _c_u64p],
+                          ctypes.c_int),
     "pg_permanent_mod3": ([_c_i64p, ctypes.c_int, _c_intp], ctypes.c_int),
     "pg_permanent_mod3_cols": ([_c_u64p, _c_u64p, ctypes.c_int, _c_intp], ctypes.c_int),
     "pg_affine_residues": ([_c_i64p, _c_i64p, ctypes.c_int, _c_u64p, ctypes.c_int, _c_u64p],
@@ -178,6 +182,44 @@ def necklace_orbit_stats(n: int) -> tuple[int, int]:
         raise ValueError(load().pg_last_error().decode())
     check(st)
     return int(reps.value), int(words.value)
+
+
+def glynn_f64_fwd_bwd(matrices, want_grad: bool = True):
+    """(per[batch], grad[batch][n][n] or None, abs_sum[batch]) for a batch of
+    real matrices through the host-pointer C entry point."""
+    a = np.ascontiguousarray(matrices, dtype=np.float64)
+    batch, n = a.shape[0], a.shape[1]
+    per = np.zeros(batch, dtype=np.float64)
+    grad = np.zeros((batch, n, n), dtype=np.float64) if want_grad else None
+    abs_sum = np.zeros(batch, dtype=np.float64)
+    check(load().pg_glynn_f64_fwd_bwd(ptr(a, ctypes.c_double), batch, n,
+                                      ptr(per, ctypes.c_double),
+                                      ptr(grad, ctypes.c_double) if want_grad else None,
+                                      ptr(abs_sum, ctypes.c_double)))
+    return per, grad, abs_sum
+
+
+def batch_residues(matrices, moduli_lists) -> list[list[int]]:
+    """[[per(A_m) mod q for q in moduli_lists[m]] for each matrix A_m]."""
+    mats = [np.ascontiguousarray(m, dtype=np.int64) for m in matrices]
+    orders = np.array([m.shape[0] if m.ndim == 2 else 0 for m in mats], dtype=np.int32)
+    offsets = np.zeros(len(mats), dtype=np.int64)
+    if len(mats) > 1:
+        offsets[1:] = np.cumsum([m.size for m in mats])[:-1]
+    flat = np.ascontiguousarray(np.concatenate([m.ravel() for m in mats]) if mats else
+                                np.zeros(1, np.int64), dtype=np.int64)
+    if flat.size == 0:
+        flat = np.zeros(1, np.int64)
+    mods = np.ascontiguousarray(np.array([int(q) for ms in moduli_lists for q in ms] or [1],
+                                         dtype=np.uint64))
+    moff = np.zeros(len(mats) + 1, dtype=np.int32)
+    moff[1:] = np.cumsum([len(ms) for ms in moduli_lists])
+    out = np.zeros(max(1, int(moff[-1])), dtype=np.uint64)
+    check(load().pg_batch_residues(ptr(flat, ctypes.c_int64), ptr(offsets, ctypes.c_int64),
+                                   ptr(orders, ctypes.c_int32), len(mats),
+                                   ptr(mods, ctypes.c_uint64), ptr(moff, ctypes.c_int32),
+                                   ptr(out, ctypes.c_uint64)))
+    return [[int(out[t]) for t in range(moff[m], moff[m + 1])] for m in range(len(mats))]
 
 
 def permanent_mod3(matrix) -> int:
