@@ -710,6 +710,18 @@ def run_gpu_exact_set(args, world, rank, local):
         want = [int(table[str(n)])]
         desc = (f"perm(S_{n}): {n - 1}x{n - 1} circulant cofactor minor, rotation+complement "
                 f"necklace orbits, primes == 1 (mod {n}) < 2^30")
+    elif args.workload == "grid40":
+        # the reference's showcase binary matrix: biadjacency of the 4x4x5
+        # grid graph, periodic in two axes (tests/golden/binary.json)
+        g = json.loads((ROOT / "tests" / "golden" / "binary.json").read_text())
+        grid = g["grid_4x4x5_periodic01"]
+        items = [grid["matrix"]]
+        states = 1 << 39
+
+        def step():
+            return [permgpu.binary_permanent(m) for m in items]
+        want = [int(grid["permanent"])]
+        desc = "40x40 biadjacency of the 4x4x5 grid, periodic in axes 0 and 1"
     else:
         mats = workloads.binary40(8)
         items = [m.tolist() for m in mats]
@@ -755,6 +767,23 @@ def run_gpu_exact_set(args, world, rank, local):
                     "note": f"whole-call API permgpu.permanent({n}) timed end to end"},
             "clocks": clk, "gpu_launches": args.steps,
         }))
+    elif rank == 0 and args.workload == "grid40":
+        # published: the reference's CUDA binary kernel, two residues plus
+        # CRT, 22.73 s end to end on a GH200 (BINARY_APPLICATIONS.md:165-171)
+        print(json.dumps({
+            "metric": "seconds to exact per(grid 4x4x5, 40x40 0/1)", "value": step_s,
+            "unit": "s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * step_s, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": step_s / 22.73, "dtype": "int32",
+            "data": "none (the matrix is the grid biadjacency)",
+            "config": {"workload": f"{args.workload}: {desc}", "states": states},
+            "steps_per_s": states / step_s, "results": [str(v) for v in got],
+            "result_checked_against_reference": True,
+            "e2e": {"value": step_s, "unit": "s", "h2d_bytes_per_step": None,
+                    "d2h_bytes_per_step": None,
+                    "note": "whole-call API permgpu.binary_permanent timed end to end"},
+            "clocks": clk, "gpu_launches": args.steps,
+        }))
     elif rank == 0:
         print(json.dumps({
             "metric": f"Glynn steps/s ({args.workload})", "value": world * states / step_s,
@@ -779,7 +808,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="generic32",
                     choices=sorted(WORKLOADS) + ["batch4096", "float28", "schur", "schur41",
-                                                 "binary40", "rook28", "mod3_40"])
+                                                 "binary40", "grid40", "rook28", "mod3_40"])
     ap.add_argument("--residue-loop-sample", type=int, default=256)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -797,7 +826,7 @@ def main():
         run_gpu_batch(args, world, rank, local)
     elif args.workload == "float28":
         run_gpu_float28(args, world, rank, local)
-    elif args.workload in ("schur", "schur41", "binary40"):
+    elif args.workload in ("schur", "schur41", "binary40", "grid40"):
         run_gpu_exact_set(args, world, rank, local)
     elif args.workload == "mod3_40":
         run_gpu_mod3(args, world, rank, local)
