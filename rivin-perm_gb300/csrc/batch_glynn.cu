@@ -138,10 +138,9 @@ static void add_i64_at(std::vector<uint32_t> &w, int pos, long long v) {
     }
 }
 
-// Row order for groups of 4 (every group's bound product < 2^31), or false.
+// Row order for groups of 4 (exact_group_rows), or false.
 static bool batch_group(const int64_t *A, int n, std::vector<int> *order) {
     const int G = n >= 4 ? 4 : n;
-    const int NG = (n + G - 1) / G;
     std::vector<uint64_t> B(n);
     for (int i = 0; i < n; i++) {
         unsigned __int128 s = 0;
@@ -152,33 +151,8 @@ static bool batch_group(const int64_t *A, int n, std::vector<int> *order) {
         if (s >= ((unsigned __int128)1 << 30)) return false;
         B[i] = (uint64_t)s;
     }
-    std::vector<int> rows(n);
-    for (int i = 0; i < n; i++) rows[i] = i;
-    std::stable_sort(rows.begin(), rows.end(), [&](int x, int y) { return B[x] > B[y]; });
-    std::vector<int> cap(NG, G);
-    cap[NG - 1] = n - (NG - 1) * G;
-    std::vector<double> lp(NG, 0.0);
-    std::vector<std::vector<int>> mem(NG);
-    for (int r : rows) {
-        int best = -1;
-        for (int g = 0; g < NG; g++) {
-            if ((int)mem[g].size() >= cap[g]) continue;
-            if (best < 0 || lp[g] < lp[best]) best = g;
-        }
-        mem[best].push_back(r);
-        lp[best] += std::log2((double)(B[r] ? B[r] : 1));
-    }
-    for (auto &g : mem) {
-        unsigned __int128 p = 1;
-        for (int r : g) {
-            p *= (B[r] ? B[r] : 1);
-            if (p >= ((unsigned __int128)1 << 31)) return false;
-        }
-    }
-    order->clear();
-    for (auto &g : mem)
-        for (int r : g) order->push_back(r);
-    return true;
+    order->resize(n);
+    return exact_group_rows(B.data(), n, G, order->data());
 }
 
 struct BatchPlan {

@@ -27,8 +27,16 @@
 #include <stdint.h>
 
 #include "acc_chain.cuh"
+#include "col_acc.cuh"
 #include "mp_mul.cuh"
 #include "mp_mul_oop.cuh"
+
+// 1: the last row group multiplies the running product into 64-bit column
+// accumulators folded every 2^LOGU terms (col_acc.cuh); 0: every term is
+// formed in full and added with its sign (acc_chain.cuh).
+#ifndef EXACT_COLACC
+#define EXACT_COLACC 1
+#endif
 
 #ifndef EXACT_MUL_OOP
 #define EXACT_MUL_OOP 0
@@ -89,6 +97,7 @@ struct ExactShape {
     static constexpr int NG = (N + G - 1) / G;           // product words
     static constexpr int NL = NG + (N > 32 ? 2 : 1);     // accumulator words
     static constexpr int LOGU = (N - 1) < EXACT_LOGU ? (N - 1) : EXACT_LOGU;
+    static constexpr int NR = NG > 1 ? NG - 1 : 1;       // words of the leading product
 };
 
 // Row sums of Gray state `start`: init - sum_{j in gray(start)} 2 a_j.
@@ -144,6 +153,52 @@ __device__ __forceinline__ void exact_term(const int32_t *s, uint32_t *acc, uint
 #endif
 }
 
+// Column form of one term: the sign and the first NG-1 group products give
+// the signed NR-word R, the last group's magnitude y multiplies R into the
+// columns (first: the columns start from this term).  For NG == 1, R = +-1.
+// R[0..K-1] (signed) *= |x[K]| ... |x[END-1]|, one word per factor.
+template <int K, int END>
+struct ProdChainS {
+    static __device__ __forceinline__ void run(uint32_t *R, const int32_t *x) {
+        MulWordS<K>::apply(R, (uint32_t)abs(x[K]));
+        ProdChainS<K + 1, END>::run(R, x);
+    }
+};
+template <int END>
+struct ProdChainS<END, END> {
+    static __device__ __forceinline__ void run(uint32_t *, const int32_t *) {}
+};
+
+template <int N, int G>
+__device__ __forceinline__ void exact_term_col(const int32_t *s, uint64_t *col, int64_t &colt,
+                                               uint32_t odd, bool first) {
+    using S = ExactShape<N, G>;
+    constexpr int NG = S::NG, NR = S::NR;
+    int32_t x[NG];
+#pragma unroll
+    for (int g = 0; g < NG; g++) {
+        x[g] = s[g * G];
+#pragma unroll
+        for (int t = 1; t < G; t++)
+            if (g * G + t < N) x[g] *= s[g * G + t];
+    }
+    uint32_t sx = odd << 31;
+#pragma unroll
+    for (int g = (NG > 1 ? 1 : 0); g < NG; g++) sx ^= (uint32_t)x[g];
+    const int32_t m = (int32_t)sx >> 31;
+    uint32_t R[NR + 1];
+    R[0] = (uint32_t)(((NG > 1 ? x[0] : 1) ^ m) - m);
+    ProdChainS<1, (NG > 1 ? NG - 1 : 1)>::run(R, x);
+    const uint32_t y = (uint32_t)abs(x[NG - 1]);
+#pragma unroll
+    for (int l = 0; l < NR - 1; l++) {
+        const uint64_t p = (uint64_t)R[l] * y;
+        col[l] = first ? p : col[l] + p;
+    }
+    const int64_t pt = (int64_t)(int32_t)R[NR - 1] * (int64_t)y;
+    colt = first ? pt : colt + pt;
+}
+
 // Walk chunks [c_begin, c_end) (row sums s already at state c_begin*2^log_len)
 // adding every term into acc.  Returns false if the abort word was seen.
 template <int N, int G>
@@ -153,6 +208,10 @@ __device__ __forceinline__ bool exact_walk(const int32_t *tab, int32_t *s, uint3
     using S = ExactShape<N, G>;
     constexpr int NP = S::NP, LOGU = S::LOGU, U = 1 << LOGU;
     const uint32_t Q = (1u << log_len) >> LOGU;
+#if EXACT_COLACC
+    uint64_t col[S::NR > 1 ? S::NR - 1 : 1];
+    int64_t colt;
+#endif
     for (uint64_t c = c_begin; c < c_end; c++) {
         if (((c - c_begin) & 255) == 0 && *abort_flag) return false;
         const uint32_t hib = (uint32_t)(c & 1) << log_len;
@@ -189,8 +248,15 @@ __device__ __forceinline__ bool exact_walk(const int32_t *tab, int32_t *s, uint3
                     }
                 }
                 // chunks start at even states, so (-1)^g = (-1)^r
+#if EXACT_COLACC
+                exact_term_col<N, G>(s, col, colt, (uint32_t)(r & 1), r == 0);
+#else
                 exact_term<N, G>(s, acc, (uint32_t)(r & 1));
+#endif
             }
+#if EXACT_COLACC
+            FoldCols<S::NR, S::NL>::apply(acc, col, colt);
+#endif
         }
     }
     return true;
@@ -302,5 +368,16 @@ cudaError_t launch_exact_any(int N, int G, const ExactArgs &args, int blocks,
                              cudaStream_t stream);
 int occupancy_exact_any(int N, int G);
 bool exact_compiled(int N, int G);
+
+// Largest bound product of the last row group: with column accumulation its
+// magnitude multiplies each word of the running product into a 64-bit
+// column 2^EXACT_LOGU times between folds.
+constexpr uint64_t EXACT_LAST_GROUP_MAX =
+    EXACT_COLACC ? (1ull << (32 - EXACT_LOGU)) : (1ull << 31) - 1;
+
+// Row order for group size G (rows [g*G, min((g+1)*G, n)) form group g) in
+// which every group's product of row bounds B is < 2^31 and the last
+// group's is <= EXACT_LAST_GROUP_MAX; n <= 48.  False if none was found.
+bool exact_group_rows(const uint64_t *B, int n, int G, int *order);
 
 }  // namespace pg

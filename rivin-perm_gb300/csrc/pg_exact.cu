@@ -12,40 +12,48 @@ namespace pg {
 
 static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
-// Row grouping for group size G: rows are permuted so that rows
-// [g*G, min((g+1)*G, n)) form group g and every group's product of row
-// bounds is < 2^31.  Returns false if no such grouping was found.
-static bool group_rows(const std::vector<uint64_t> &B, int n, int G,
-                       std::vector<int> *order) {
+// Greedy grouping: rows in descending bound order, each into the open group
+// with the smallest log-product.  With small_last the last group is first
+// filled with the rows of smallest bound (it multiplies into the columns).
+static bool try_grouping(const uint64_t *B, int n, int G, bool small_last, int *order) {
     const int NG = (n + G - 1) / G;
-    std::vector<int> cap(NG, G);
-    cap[NG - 1] = n - (NG - 1) * G;
-    std::vector<int> rows(n);
-    for (int i = 0; i < n; i++) rows[i] = i;
-    std::stable_sort(rows.begin(), rows.end(),
-                     [&](int x, int y) { return B[x] > B[y]; });
-    std::vector<double> logp(NG, 0.0);
-    std::vector<std::vector<int>> members(NG);
-    for (int r : rows) {
+    const int last_cap = n - (NG - 1) * G;
+    int idx[48], cnt[48] = {0}, mem[48][8];
+    double lp[48] = {0};
+    for (int i = 0; i < n; i++) idx[i] = i;
+    for (int i = 1; i < n; i++)                    // stable, descending B
+        for (int k = i; k > 0 && B[idx[k]] > B[idx[k - 1]]; k--) std::swap(idx[k], idx[k - 1]);
+    int rows = n;
+    if (small_last && NG > 1) {
+        for (int t = 0; t < last_cap; t++) mem[NG - 1][cnt[NG - 1]++] = idx[n - 1 - t];
+        rows = n - last_cap;
+    }
+    for (int i = 0; i < rows; i++) {
         int best = -1;
         for (int g = 0; g < NG; g++) {
-            if ((int)members[g].size() >= cap[g]) continue;
-            if (best < 0 || logp[g] < logp[best]) best = g;
+            if (cnt[g] >= (g == NG - 1 ? last_cap : G)) continue;
+            if (best < 0 || lp[g] < lp[best]) best = g;
         }
-        members[best].push_back(r);
-        logp[best] += std::log2((double)(B[r] ? B[r] : 1));
+        mem[best][cnt[best]++] = idx[i];
+        lp[best] += std::log2((double)(B[idx[i]] ? B[idx[i]] : 1));
     }
     for (int g = 0; g < NG; g++) {
         unsigned __int128 prod = 1;
-        for (int r : members[g]) {
-            prod *= (B[r] ? B[r] : 1);
+        for (int t = 0; t < cnt[g]; t++) {
+            prod *= (B[mem[g][t]] ? B[mem[g][t]] : 1);
             if (prod >= ((unsigned __int128)1 << 31)) return false;
         }
+        if (g == NG - 1 && prod > EXACT_LAST_GROUP_MAX) return false;
     }
-    order->clear();
+    int w = 0;
     for (int g = 0; g < NG; g++)
-        for (int r : members[g]) order->push_back(r);
+        for (int t = 0; t < cnt[g]; t++) order[w++] = mem[g][t];
     return true;
+}
+
+bool exact_group_rows(const uint64_t *B, int n, int G, int *order) {
+    if (n < 1 || n > 48 || G < 1 || G > 8) return false;
+    return try_grouping(B, n, G, false, order) || try_grouping(B, n, G, true, order);
 }
 
 // Picks the largest compiled group size that admits a grouping.
@@ -61,9 +69,10 @@ static int choose_group(const int64_t *A, int n, std::vector<int> *order) {
         if (s >= ((unsigned __int128)1 << 30)) return 0;
         B[i] = (uint64_t)s;
     }
+    order->resize(n);
     for (int G = 6; G >= 1; G--) {
         if (!exact_compiled(n, G)) continue;
-        if (group_rows(B, n, G, order)) return G;
+        if (exact_group_rows(B.data(), n, G, order->data())) return G;
     }
     return 0;
 }

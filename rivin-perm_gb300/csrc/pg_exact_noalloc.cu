@@ -87,38 +87,7 @@ extern "C" int pg_exact_permanent_noalloc(const int64_t *A, int n, uint32_t *out
     int order[48], G = 0;
     for (int g = 6; g >= 1 && !G; g--) {
         if (!exact_compiled(n, g)) continue;
-        // greedy: largest bound into the group with the smallest log-product
-        const int NG = (n + g - 1) / g;
-        int cnt[48] = {0}, members[48][6];
-        double lp[48] = {0};
-        int idx[48];
-        for (int i = 0; i < n; i++) idx[i] = i;
-        for (int i = 1; i < n; i++)            // insertion sort, descending B
-            for (int k = i; k > 0 && B[idx[k]] > B[idx[k - 1]]; k--) {
-                const int t = idx[k]; idx[k] = idx[k - 1]; idx[k - 1] = t;
-            }
-        for (int i = 0; i < n; i++) {
-            int best = -1;
-            for (int q = 0; q < NG; q++) {
-                const int cap = q == NG - 1 ? n - (NG - 1) * g : g;
-                if (cnt[q] >= cap) continue;
-                if (best < 0 || lp[q] < lp[best]) best = q;
-            }
-            members[best][cnt[best]++] = idx[i];
-            lp[best] += std::log2(B[idx[i]] ? (double)B[idx[i]] : 1.0);
-        }
-        bool fits = true;
-        for (int q = 0; q < NG && fits; q++) {
-            unsigned __int128 p = 1;
-            for (int t = 0; t < cnt[q]; t++) {
-                p *= B[members[q][t]] ? B[members[q][t]] : 1;
-                if (p >= ((unsigned __int128)1 << 31)) { fits = false; break; }
-            }
-        }
-        if (!fits) continue;
-        int w = 0;
-        for (int q = 0; q < NG; q++)
-            for (int t = 0; t < cnt[q]; t++) order[w++] = members[q][t];
+        if (!exact_group_rows(B, n, g, order)) continue;
         G = g;
     }
     if (!G) return fail(PG_EOVERFLOW, "row-sum bound exceeds the exact engine's fixed widths");

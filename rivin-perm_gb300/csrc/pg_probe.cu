@@ -26,7 +26,12 @@ __global__ void __launch_bounds__(256) imad_probe_kernel(uint32_t seed, int iter
 #pragma unroll
         for (int c = 0; c < 8; c++) {
             if (V == 0) asm volatile("mad.lo.u32 %0, %0, %1, %2;" : "+r"(x[c]) : "r"(y), "r"(c + 1u));
-            if (V == 1) asm volatile("mad.wide.u32 %0, %1, %2, %0;" : "+l"(w[c]) : "r"(x[c]), "r"(y));
+            // the multiplicand is the low word of the running sum, so every
+            // product depends on the previous one and none can be hoisted
+            if (V == 1)
+                asm volatile("{\n\t.reg .u32 lo, hi;\n\tmov.b64 {lo, hi}, %0;\n\t"
+                             "mad.wide.u32 %0, lo, %1, %0;\n\t}"
+                             : "+l"(w[c]) : "r"(y));
             if (V == 2) asm volatile("mad.hi.u32 %0, %0, %1, %2;" : "+r"(x[c]) : "r"(y), "r"(c + 7u));
             if (V == 3) asm volatile("add.u32 %0, %0, %1;" : "+r"(x[c]) : "r"(y));
         }
