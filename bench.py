@@ -253,7 +253,8 @@ def run_gpu(args, world, rank, local):
 
     # IMAD roofline denominators (measured live)
     peak_lo = _lib.probe_int_throughput(0)
-    peak_wide = _lib.probe_int_throughput(1)
+    peak_madw = _lib.probe_int_throughput(1)     # mad.wide.u32, 64-bit addend
+    peak_mulw = _lib.probe_int_throughput(4)     # mul.wide.u32, no addend
 
     clocks = ClockSampler(local).start()
     barrier(world)
@@ -292,9 +293,19 @@ def run_gpu(args, world, rank, local):
     value = world * states / (step_ms * 1e-3)
     e2e_value = world * states / e2e_step
     # roofline: IMAD-pipe work counted from the kernel source, in mad.lo.u32
-    # equivalents (mad.wide.u32 weighted by the measured rate ratio)
-    wide_weight = peak_lo / peak_wide
-    slots = plan.imul_per_state + plan.imad_wide_per_state * wide_weight
+    # equivalents.  With NG product words a term is n - NG IMUL (row-group
+    # products), (NG-2)(NG-1)/2 mul.wide.u32 (the running product) and
+    # max(NG-1, 1) mad.wide.u32 into the 64-bit columns.  Every 32x32->64
+    # product is weighted by the measured mul.wide.u32 : mad.lo.u32 rate
+    # ratio (about 2).  The mad.wide probe (64-bit addend) runs slower still
+    # in isolation, but inside the kernels splitting it into mul.wide plus an
+    # ALU add was slower, so it is counted at the mul.wide weight (the
+    # conservative choice: a larger weight would raise the fraction).
+    ng = plan.words
+    n_mulw = (ng - 2) * (ng - 1) // 2 if ng >= 2 else 0
+    n_madw = max(ng - 1, 1)
+    w_mulw = peak_lo / peak_mulw
+    slots = plan.imul_per_state + (n_mulw + n_madw) * w_mulw
     achieved = states * slots / (statistics.mean(kernel_ms) * 1e-3)
     NP = (n + 3) & ~3
     h2d = (n - 1) * 2 * NP * 4 + NP * 4
@@ -326,9 +337,10 @@ def run_gpu(args, world, rank, local):
                          "peak_source": "measured live: pg_probe_int_throughput mad.lo.u32 "
                                         "(no integer peak in MEASURED_PEAKS.json)",
                          "work_per_state": {"imul": plan.imul_per_state,
-                                            "mad_wide": plan.imad_wide_per_state,
-                                            "mad_wide_weight": wide_weight},
-                         "mad_wide_ops_per_s": peak_wide},
+                                            "mul_wide": n_mulw, "mad_wide": n_madw,
+                                            "wide_weight": w_mulw, "slots": slots},
+                         "probe_ops_per_s": {"mad.lo.u32": peak_lo, "mul.wide.u32": peak_mulw,
+                                             "mad.wide.u32": peak_madw}},
             "cpu_baseline": None if cpu_rate is None else {
                 "value": cpu_rate, "unit": "steps/s", "cores": cores, "kind": kind,
                 "sample": sample},
@@ -535,15 +547,20 @@ def run_gpu_poly(args, world, rank, local):
     bounds = poly._bounds(tuple((1,) * n for _ in range(n)), am)
     primes = poly._gpu_primes(max(bounds))
     states = len(primes) * (1 << (n - 1))
-    # IMAD-class instructions per state: factor r = 1..n-1 costs two plain
-    # reductions (3 each) and r fused two-product reductions (4 each)
+    # IMAD-pipe work per state in mad.lo.u32 slots: factor r = 1..n-1 costs
+    # two plain reductions (mul.wide, mul.lo, mad.wide) and r fused
+    # two-product reductions (mul.wide, mad.wide, mul.lo, mad.wide); every
+    # 32x32->64 product is weighted by the measured mul.wide : mad.lo ratio
     imad_per_state = 2 * (n - 1) * (n + 3)
     for _ in range(args.warmup):
         got = permgpu.rook_polynomial(a.tolist())
         _lib.affine_residues(ones, a, primes)
     if got[1] != int(a.sum()):
         raise SystemExit("rook polynomial failed its r_1 = #ones check")
-    peak = _lib.probe_int_throughput(0) / 1e12    # mad.lo.u32 ops/s -> Tops/s
+    peak_lo = _lib.probe_int_throughput(0)
+    peak = peak_lo / 1e12                         # mad.lo.u32 ops/s -> Tops/s
+    w = peak_lo / _lib.probe_int_throughput(4)    # mul.wide.u32 weight
+    slots_per_state = 2 * (n - 1) * (2 * w + 1) + (3 * w + 1) * (n - 1) * n / 2
     clocks = ClockSampler(local).start()
     barrier(world)
     ts, te = [], []
@@ -581,7 +598,7 @@ def run_gpu_poly(args, world, rank, local):
                          f"{len(primes)} primes x 2^{n - 1} states",
                "time_to_exact_s_est": states / per_prime}
     if rank == 0:
-        achieved = states * imad_per_state / step_s / 1e12
+        achieved = states * slots_per_state / step_s / 1e12
         print(json.dumps({
             "metric": "polynomial Glynn prime-states/s (rook28)", "value": world * states / step_s,
             "unit": "prime-states/s", "n_gpus": world, "steps": args.steps,
@@ -595,7 +612,8 @@ def run_gpu_poly(args, world, rank, local):
             "roofline": {"bound": "imad", "achieved": achieved, "peak": peak, "unit": "Tops/s",
                          "frac": achieved / peak, "traffic": None,
                          "peak_source": "measured live: pg_probe_int_throughput mad.lo.u32",
-                         "work_per_state": {"imad_class": imad_per_state}},
+                         "work_per_state": {"imad_class_instructions": imad_per_state,
+                                            "wide_weight": w, "slots": slots_per_state}},
             "cpu_baseline": cpu,
             "e2e": {"value": world * states / e2e_s, "unit": "prime-states/s",
                     "h2d_bytes_per_step": 2 * 8 * n * n, "d2h_bytes_per_step": 8 * (n + 1) * len(primes),

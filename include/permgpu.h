@@ -292,8 +292,9 @@ int pg_exact_permanent_noalloc(const int64_t *A, int n, uint32_t *out,
 
 /*
  * Integer-pipe throughput probe (roofline denominator; no reference
- * counterpart): variant 0 mad.lo.u32, 1 mad.wide.u32, 2 mad.hi.u32,
- * 3 add.u32; writes thread-instructions per second for the whole GPU.
+ * counterpart): variant 0 mad.lo.u32, 1 mad.wide.u32 (64-bit addend),
+ * 2 mad.hi.u32, 3 add.u32, 4 mul.wide.u32 (no addend); writes
+ * thread-instructions per second for the whole GPU.
  */
 int pg_probe_int_throughput(int variant, int iters, double *ops_per_second);
 

@@ -4,9 +4,10 @@
 // form for `iters` iterations over a grid of 4 x SMs blocks x 256 threads,
 // timed with CUDA events.  Variants:
 //   0  mad.lo.u32   (32-bit multiply-add, low word)
-//   1  mad.wide.u32 (32x32 -> 64-bit multiply-add)
+//   1  mad.wide.u32 (32x32 -> 64-bit multiply-add; one ALU prmt beside it)
 //   2  mad.hi.u32   (high word)
 //   3  add.u32      (integer ALU add, for the mix reference)
+//   4  mul.wide.u32 (32x32 -> 64-bit product, no addend; one ALU xor beside it)
 // Returns operations per second (one op = one instruction for one thread).
 #include "pg_internal.h"
 
@@ -26,13 +27,23 @@ __global__ void __launch_bounds__(256) imad_probe_kernel(uint32_t seed, int iter
 #pragma unroll
         for (int c = 0; c < 8; c++) {
             if (V == 0) asm volatile("mad.lo.u32 %0, %0, %1, %2;" : "+r"(x[c]) : "r"(y), "r"(c + 1u));
-            // the multiplicand is the low word of the running sum, so every
-            // product depends on the previous one and none can be hoisted
+            // the multiplicand is byte-rotated every iteration (prmt, an
+            // ALU-pipe instruction independent of the running sum), so no
+            // product can be hoisted, the only dependency through the sum is
+            // the 64-bit addend, and the IMAD pipe executes only the mad.wide
             if (V == 1)
-                asm volatile("{\n\t.reg .u32 lo, hi;\n\tmov.b64 {lo, hi}, %0;\n\t"
-                             "mad.wide.u32 %0, lo, %1, %0;\n\t}"
-                             : "+l"(w[c]) : "r"(y));
+                asm volatile("prmt.b32 %1, %1, 0, 0x0321;\n\t"
+                             "mad.wide.u32 %0, %1, %2, %0;"
+                             : "+l"(w[c]), "+r"(x[c]) : "r"(y));
             if (V == 2) asm volatile("mad.hi.u32 %0, %0, %1, %2;" : "+r"(x[c]) : "r"(y), "r"(c + 7u));
+            // mul.wide.u32 without an addend: the next multiplicand is the
+            // XOR of the product's halves (one ALU-pipe lop3)
+            if (V == 4)
+                asm volatile("{\n\t.reg .u64 t;\n\t.reg .u32 lo, hi;\n\t"
+                             "mul.wide.u32 t, %0, %1;\n\t"
+                             "mov.b64 {lo, hi}, t;\n\t"
+                             "xor.b32 %0, lo, hi;\n\t}"
+                             : "+r"(x[c]) : "r"(y));
             if (V == 3) asm volatile("add.u32 %0, %0, %1;" : "+r"(x[c]) : "r"(y));
         }
     }
@@ -46,7 +57,7 @@ __global__ void __launch_bounds__(256) imad_probe_kernel(uint32_t seed, int iter
 
 extern "C" int pg_probe_int_throughput(int variant, int iters, double *ops_per_second) {
     using namespace pg;
-    if (!ops_per_second || variant < 0 || variant > 3 || iters < 1)
+    if (!ops_per_second || variant < 0 || variant > 4 || iters < 1)
         return fail(PG_EINVAL, "bad probe arguments");
     DeviceInfo dev;
     int st = device_info(&dev);
@@ -66,6 +77,7 @@ extern "C" int pg_probe_int_throughput(int variant, int iters, double *ops_per_s
         case 0: imad_probe_kernel<0><<<blocks, 256, 0, ws->stream>>>(rep, iters, sink); break;
         case 1: imad_probe_kernel<1><<<blocks, 256, 0, ws->stream>>>(rep, iters, sink); break;
         case 2: imad_probe_kernel<2><<<blocks, 256, 0, ws->stream>>>(rep, iters, sink); break;
+        case 4: imad_probe_kernel<4><<<blocks, 256, 0, ws->stream>>>(rep, iters, sink); break;
         default: imad_probe_kernel<3><<<blocks, 256, 0, ws->stream>>>(rep, iters, sink); break;
         }
         PG_CUDA(cudaGetLastError());
