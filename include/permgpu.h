@@ -82,7 +82,8 @@ int pg_schur_residues(int n, const uint64_t *primes, const uint64_t *omegas,
  * else the Glynn cofactor minor, else the full matrix.  PG_SCHUR_GLYNN
  * forces the cofactor minor (2^(n-2) Glynn states).  PG_SCHUR_NECKLACE
  * requires the necklace preconditions (odd prime n < 64, odd modulus
- * < 2^30, omega^n == 1) for every modulus and returns PG_ERANGE otherwise: the
+ * < 2^30, or < 2^32 for n = 37, 41, 43, 47, 53, omega^n == 1) for every
+ * modulus and returns PG_ERANGE otherwise: the
  * (n-1)x(n-1) cofactor minor is circulant in primitive-root order and its
  * 2^(n-1) Glynn sign words collapse to rotation+complement orbits, about
  * 2^(n-1)/(2(n-1)) terms.  Replaces the necklace branch of

@@ -104,10 +104,16 @@ constexpr uint64_t NECKLACE_PRIME_LIMIT = 1ull << 30;
 // Smallest order the automatic Schur dispatch sends to the necklace kernel;
 // below it the Glynn cofactor kernel finishes first.
 constexpr int NECKLACE_AUTO_MIN_ORDER = 37;
+// Odd moduli 2^30 <= p < 2^32 take the wide-modulus necklace kernel, which
+// is compiled for the orders of necklace_wide_supported (n >= 37).
+constexpr uint64_t NECKLACE_WIDE_PRIME_LIMIT = 1ull << 32;
 // True when n - 1 is a compiled necklace minor order (n an odd prime < 64).
 bool necklace_supported(int n);
+// True when the wide-modulus necklace kernel is compiled for order n.
+bool necklace_wide_supported(int n);
 // out[t] = perm(S_n) mod primes[t] for odd primes[t] < NECKLACE_PRIME_LIMIT
-// with omegas[t]^n == 1; n must satisfy necklace_supported(n).
+// (< NECKLACE_WIDE_PRIME_LIMIT when necklace_wide_supported(n)) with
+// omegas[t]^n == 1; n must satisfy necklace_supported(n).
 int schur_necklace_residues(int n, const uint64_t *primes, const uint64_t *omegas, int k,
                             uint64_t *out);
 

@@ -335,8 +335,28 @@ __host__ __device__ constexpr int nk_stride(int L) {
 
 // Moduli of the necklace kernel: a row sum is summed lazily from two terms
 // below p (< 2p), and the Montgomery chain stays below 2p as long as
-// 4p < 2^32: NECKLACE_PRIME_LIMIT = 2^30.
+// 4p < 2^32: NECKLACE_PRIME_LIMIT = 2^30.  The wide form (W) takes odd
+// moduli up to 2^32 (the reference's 32-bit pseudo-Mersenne primes) and
+// keeps every value fully reduced, with 33-bit intermediate sums.
 constexpr uint64_t NK_PRIME_LIMIT = NECKLACE_PRIME_LIMIT;
+
+// (a + b) mod p for a, b < p < 2^32
+__device__ __forceinline__ uint32_t nk_addmod_w(uint32_t a, uint32_t b, uint32_t p) {
+    const uint64_t s = (uint64_t)a + b;
+    return s >= p ? (uint32_t)(s - p) : (uint32_t)s;
+}
+
+// a * b * 2^-32 mod p for a, b < p < 2^32, fully reduced.  With
+// m = -t p^-1 mod 2^32 the low words of t and m*p add to 0 or exactly 2^32
+// (a carry iff lo(t) != 0), and (t + m*p) / 2^32 < 2p needs 33 bits.
+__device__ __forceinline__ uint32_t nk_redc_w(uint32_t a, uint32_t b, uint32_t p,
+                                              uint32_t pinv) {
+    const uint64_t t = (uint64_t)a * b;
+    const uint32_t m = (uint32_t)t * pinv;
+    const uint64_t mp = (uint64_t)m * p;
+    const uint64_t u = (t >> 32) + (mp >> 32) + ((uint32_t)t != 0u);
+    return u >= p ? (uint32_t)(u - p) : (uint32_t)u;
+}
 
 struct NeckArgs {
     // [k][256][LS]: entry (v, x) = sum over set bits t of the byte v of
@@ -357,7 +377,7 @@ struct NeckArgs {
 
 constexpr int NK_CHAINS = 4;      // Montgomery chains per term
 
-template <int L>
+template <int L, bool W = false>
 struct NeckLane {
     static constexpr int LS = nk_stride(L);
     static constexpr int NCH = (L + 7) / 8;                     // bytes of an L-bit word
@@ -384,7 +404,7 @@ struct NeckLane {
 #pragma unroll
             for (int r = 0; r < L; r++) {
                 const uint32_t d = t[(r + 8 * j) % L];
-                hm[r] = m32_addmod(hm[r], d - p, p);
+                hm[r] = W ? nk_addmod_w(hm[r], d, p) : m32_addmod(hm[r], d - p, p);
             }
         }
         cur = 0;
@@ -405,7 +425,7 @@ struct NeckLane {
             for (int r = 0; r < L; r++) {
                 const uint32_t x = tn[(r + 8 * j) % L], y = to[(r + 8 * j) % L];
                 const uint32_t d = x >= y ? x - y : x - y + p;     // (x - y) mod p
-                hm[r] = m32_addmod(hm[r], d - p, p);
+                hm[r] = W ? nk_addmod_w(hm[r], d, p) : m32_addmod(hm[r], d - p, p);
             }
         }
         cur = nw;
@@ -415,6 +435,14 @@ struct NeckLane {
     // byte 0 (< 2p).
     __device__ __forceinline__ void eval(const uint32_t *tab, uint32_t e, uint32_t orbit) {
         const uint32_t *t0 = tab + (e & 0xff) * LS;
+        // narrow: lazy sums below 2p and the chain of the residue kernel;
+        // wide: fully reduced sums and products
+        const auto add2 = [&](uint32_t x, uint32_t y) {
+            return W ? nk_addmod_w(x, y, p) : x + y;
+        };
+        const auto mul = [&](uint32_t x, uint32_t y) {
+            return W ? nk_redc_w(x, y, p, pinv) : m32_redc_mul(x, y, p, pinv);
+        };
         uint32_t prod;
         if constexpr (L >= 8) {
             // C independent Montgomery chains (ILP), joined by a pairwise
@@ -427,39 +455,39 @@ struct NeckLane {
                 uint32_t sr[V];
                 if constexpr (V == 4) {
                     const uint4 x = *reinterpret_cast<const uint4 *>(t0 + 4 * q);
-                    sr[0] = hm[4 * q] + x.x; sr[1] = hm[4 * q + 1] + x.y;
-                    sr[2] = hm[4 * q + 2] + x.z; sr[3] = hm[4 * q + 3] + x.w;
+                    sr[0] = add2(hm[4 * q], x.x); sr[1] = add2(hm[4 * q + 1], x.y);
+                    sr[2] = add2(hm[4 * q + 2], x.z); sr[3] = add2(hm[4 * q + 3], x.w);
                 } else {
                     const uint2 x = *reinterpret_cast<const uint2 *>(t0 + 2 * q);
-                    sr[0] = hm[2 * q] + x.x; sr[1] = hm[2 * q + 1] + x.y;
+                    sr[0] = add2(hm[2 * q], x.x); sr[1] = add2(hm[2 * q + 1], x.y);
                 }
 #pragma unroll
                 for (int i = 0; i < V; i++) {
                     const int r = V * q + i;
                     if (r < C) ch[r] = sr[i];
-                    else ch[r % C] = m32_redc_mul(ch[r % C], sr[i], p, pinv);
+                    else ch[r % C] = mul(ch[r % C], sr[i]);
                 }
             }
 #pragma unroll
             for (int w = 1; w < C; w *= 2)
 #pragma unroll
                 for (int i = 0; i + w < C; i += 2 * w)
-                    ch[i] = m32_redc_mul(ch[i], __viaddmin_u32(ch[i + w], 0u - p, ch[i + w]), p, pinv);
+                    ch[i] = mul(ch[i], W ? ch[i + w] : __viaddmin_u32(ch[i + w], 0u - p, ch[i + w]));
             prod = ch[0];
         } else {
-            // L < 8: one byte; reduce each row sum (< 2p) and chain serially
+            // L < 8: one byte; reduce each row sum and chain serially
             prod = 0;
 #pragma unroll
             for (int r = 0; r < L; r++) {
-                uint32_t sr = hm[r] + t0[r];
-                sr = __viaddmin_u32(sr, 0u - p, sr);
-                prod = r == 0 ? sr : m32_redc_mul(prod, sr, p, pinv);
+                uint32_t sr = add2(hm[r], t0[r]);
+                if (!W) sr = __viaddmin_u32(sr, 0u - p, sr);
+                prod = r == 0 ? sr : mul(prod, sr);
             }
         }
         // prod * orbit < 2p * 120 < 256p: an odd-weight term adds 256p - v
         const unsigned long long v = (unsigned long long)prod * orbit;
         acc += (e >> 31) ? ((unsigned long long)p << 8) - v : v;
-        if (++count == (1u << 20)) {     // each addend < 2^36: reduce long before 2^64
+        if (++count == (1u << 20)) {     // each addend < 2^40: reduce long before 2^64
             acc %= p;
             count = 0;
         }
@@ -488,7 +516,7 @@ struct NkQueue {
 constexpr int NK_QUEUE = 4;        // accepted words a lane may hold
 constexpr int NK_WALK_STEPS = 3;   // walker steps per evaluation (about 2.5 steps per word)
 
-template <int L>
+template <int L, bool W>
 __global__ void __launch_bounds__(256) necklace_m32_kernel(NeckArgs a) {
     constexpr int LS = nk_stride(L);
     extern __shared__ uint4 nsm[];
@@ -499,7 +527,7 @@ __global__ void __launch_bounds__(256) necklace_m32_kernel(NeckArgs a) {
     }
     __syncthreads();
     const uint32_t *tab = reinterpret_cast<const uint32_t *>(nsm);
-    NeckLane<L> lane;
+    NeckLane<L, W> lane;
     lane.p = a.moduli[k];
     lane.pinv = a.pinvs[k];
     lane.acc = 0;
@@ -561,6 +589,9 @@ __global__ void __launch_bounds__(256) necklace_m32_kernel(NeckArgs a) {
 // beyond any run anyway).
 #define PG_NK_ORDERS(X) X(2) X(4) X(6) X(10) X(12) X(16) X(18) X(22) X(28) X(30) \
                         X(36) X(40) X(42) X(46) X(52)
+// Orders with the wide-modulus kernel (odd moduli 2^30 <= p < 2^32): the
+// orders of the automatic necklace dispatch (n >= 37).
+#define PG_NK_WIDE_ORDERS(X) X(36) X(40) X(42) X(46) X(52)
 
 bool necklace_supported(int n) {
     switch (n - 1) {
@@ -573,26 +604,47 @@ bool necklace_supported(int n) {
     }
 }
 
-static cudaError_t launch_necklace(int L, const NeckArgs &a, int k, int sm_count,
-                                   cudaStream_t s) {
-    const size_t smem = (size_t)256 * nk_stride(L) * 4;
-    switch (L) {
-#define PG_NK_CASE(LL)                                                                    \
-    case LL: {                                                                            \
-        cudaError_t e = cudaFuncSetAttribute(necklace_m32_kernel<LL>,                     \
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                                             (int)smem);                                  \
-        if (e != cudaSuccess) return e;                                                   \
-        int per_sm = 0;                                                                   \
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, necklace_m32_kernel<LL>, \
-                                                          256, smem);                     \
-        if (e != cudaSuccess) return e;                                                   \
-        if (per_sm < 1) per_sm = 1;                                                       \
-        int bpm = (per_sm * sm_count + k - 1) / k;                                        \
-        dim3 grid(bpm, k);                                                                \
-        necklace_m32_kernel<LL><<<grid, 256, smem, s>>>(a);                               \
-        return cudaGetLastError();                                                        \
+bool necklace_wide_supported(int n) {
+    switch (n - 1) {
+#define PG_NK_YES(LL) case LL:
+        PG_NK_WIDE_ORDERS(PG_NK_YES)
+#undef PG_NK_YES
+        return true;
+    default:
+        return false;
     }
+}
+
+template <int L, bool W>
+static cudaError_t launch_necklace_t(const NeckArgs &a, int k, int sm_count, cudaStream_t s) {
+    const size_t smem = (size_t)256 * nk_stride(L) * 4;
+    cudaError_t e = cudaFuncSetAttribute(necklace_m32_kernel<L, W>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, necklace_m32_kernel<L, W>, 256,
+                                                      smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
+    const int bpm = (per_sm * sm_count + k - 1) / k;
+    dim3 grid(bpm, k);
+    necklace_m32_kernel<L, W><<<grid, 256, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+static cudaError_t launch_necklace(int L, bool wide, const NeckArgs &a, int k, int sm_count,
+                                   cudaStream_t s) {
+    if (wide) {
+        switch (L) {
+#define PG_NK_CASE(LL) case LL: return launch_necklace_t<LL, true>(a, k, sm_count, s);
+            PG_NK_WIDE_ORDERS(PG_NK_CASE)
+#undef PG_NK_CASE
+        default:
+            return cudaErrorInvalidValue;
+        }
+    }
+    switch (L) {
+#define PG_NK_CASE(LL) case LL: return launch_necklace_t<LL, false>(a, k, sm_count, s);
         PG_NK_ORDERS(PG_NK_CASE)
 #undef PG_NK_CASE
     default:
@@ -620,26 +672,17 @@ static int primitive_root_of_prime(int q) {
     return -1;
 }
 
-// n * per(circulant Schur minor) mod primes[t] = perm(S_n) mod primes[t],
-// for prime n with necklace_supported(n), odd primes[t] < NK_PRIME_LIMIT and
-// omegas[t]^n == 1 (mod primes[t]).
-int schur_necklace_residues(int n, const uint64_t *primes, const uint64_t *omegas, int k,
-                            uint64_t *out) {
-    if (k <= 0) return PG_OK;
+// One launch over k primes of one width (wide: 2^30 <= p < 2^32).
+static int necklace_group(int n, int g, const std::vector<uint64_t> &roots,
+                          const uint64_t *primes, const uint64_t *omegas, int k, bool wide,
+                          uint64_t *out) {
     const int L = n - 1, LS = nk_stride(L);
-    const int g = primitive_root_of_prime(n);
-    if (g < 0 || !necklace_supported(n)) return fail(PG_EINTERNAL, "necklace order not supported");
-    for (int t = 0; t < k; t++)
-        if (!(primes[t] & 1) || primes[t] >= NK_PRIME_LIMIT)
-            return fail(PG_EINTERNAL, "necklace modulus must be odd and below 2^30");
     DeviceInfo dev;
     int st = device_info(&dev);
     if (st != PG_OK) return st;
     volatile int *abort_dev;
     st = abort_flag_device(&abort_dev);
     if (st != PG_OK) return st;
-    const int depth = nk_depth(L);
-    const std::vector<uint64_t> roots = nk_roots(L, depth);
 
     const size_t tab_words = (size_t)256 * LS;
     const size_t off_s0 = nk_align((size_t)k * tab_words * 4);
@@ -699,7 +742,7 @@ int schur_necklace_residues(int n, const uint64_t *primes, const uint64_t *omega
     a.status = (int *)(d + off_status);
     PG_CUDA(cudaMemcpyAsync(d, h, off_cnt, cudaMemcpyHostToDevice, ws->stream));
     PG_CUDA(cudaMemsetAsync(d + off_cnt, 0, total - off_cnt, ws->stream));
-    PG_CUDA(launch_necklace(L, a, k, dev.sm_count, ws->stream));
+    PG_CUDA(launch_necklace(L, wide, a, k, dev.sm_count, ws->stream));
     PG_CUDA(cudaMemcpyAsync(h + off_acc, d + off_acc, total - off_acc, cudaMemcpyDeviceToHost,
                             ws->stream));
     PG_CUDA(cudaStreamSynchronize(ws->stream));
@@ -711,6 +754,39 @@ int schur_necklace_residues(int n, const uint64_t *primes, const uint64_t *omega
         if (L >= 2) r = mulmod_u64(r, powmod_u64((1ull << 32) % p, (uint64_t)(L - 1), p), p);
         r = mulmod_u64(r, powmod_u64((p >> 1) + 1, (uint64_t)L, p), p);   // 2^-L
         out[t] = mulmod_u64(r, (uint64_t)n % p, p);
+    }
+    return PG_OK;
+}
+
+// n * per(circulant Schur minor) mod primes[t] = perm(S_n) mod primes[t],
+// for prime n with necklace_supported(n), odd primes[t] < NK_PRIME_LIMIT (or
+// < 2^32 when necklace_wide_supported(n)) and omegas[t]^n == 1 (mod
+// primes[t]).  Narrow and wide moduli run as two launches.
+int schur_necklace_residues(int n, const uint64_t *primes, const uint64_t *omegas, int k,
+                            uint64_t *out) {
+    if (k <= 0) return PG_OK;
+    const int g = primitive_root_of_prime(n);
+    if (g < 0 || !necklace_supported(n)) return fail(PG_EINTERNAL, "necklace order not supported");
+    std::vector<uint64_t> pw[2], ww[2], res[2];
+    std::vector<int> idx[2];
+    for (int t = 0; t < k; t++) {
+        const bool wide = primes[t] >= NK_PRIME_LIMIT;
+        if (!(primes[t] & 1) || primes[t] >= NECKLACE_WIDE_PRIME_LIMIT ||
+            (wide && !necklace_wide_supported(n)))
+            return fail(PG_EINTERNAL, "necklace modulus must be odd and below 2^30 "
+                                      "(2^32 for the wide orders)");
+        pw[wide].push_back(primes[t]);
+        ww[wide].push_back(omegas[t]);
+        idx[wide].push_back(t);
+    }
+    const std::vector<uint64_t> roots = nk_roots(n - 1, nk_depth(n - 1));
+    for (int w = 0; w < 2; w++) {
+        if (pw[w].empty()) continue;
+        res[w].assign(pw[w].size(), 0);
+        const int st = necklace_group(n, g, roots, pw[w].data(), ww[w].data(),
+                                      (int)pw[w].size(), w == 1, res[w].data());
+        if (st != PG_OK) return st;
+        for (size_t i = 0; i < idx[w].size(); i++) out[idx[w][i]] = res[w][i];
     }
     return PG_OK;
 }

@@ -518,10 +518,13 @@ int pg_schur_residues_method(int n, const uint64_t *primes, const uint64_t *omeg
         const uint64_t w = omegas[t] % p;
         const bool cofactor =
             n >= 3 && (n & 1) && (p & 1) && powmod_u64(w, (uint64_t)n, p) == 1 % p;
-        const bool necklace = cofactor && necklace_supported(n) && p < NECKLACE_PRIME_LIMIT;
+        const bool necklace =
+            cofactor && necklace_supported(n) &&
+            (p < NECKLACE_PRIME_LIMIT ||
+             (p < NECKLACE_WIDE_PRIME_LIMIT && necklace_wide_supported(n)));
         if (method == PG_SCHUR_NECKLACE && !necklace)
             return fail(PG_ERANGE, "necklace quotient needs an odd prime n < 64, an odd "
-                                   "modulus below 2^30 and omega^n == 1");
+                                   "modulus below 2^30 (2^32 for n >= 37) and omega^n == 1");
         if (necklace && (method == PG_SCHUR_NECKLACE ||
                          (method == PG_SCHUR_AUTO && n >= NECKLACE_AUTO_MIN_ORDER))) {
             neck_of.push_back(t);

@@ -74,10 +74,42 @@ def test_auto_method_agrees_with_both_paths(lib):
         assert auto == _lib.schur_residues(n, primes, omegas, method="necklace")
         if n < 37:
             assert auto == _lib.schur_residues(n, primes, omegas, method="glynn")
-    # a modulus above 2^30 takes the Glynn minor under "auto"
+    # a modulus above 2^30 takes the wide-modulus necklace kernel under
+    # "auto" (n >= 37); it must agree with the Glynn minor
     primes = plan_schur(37)[0][:1] + [p for p in plan_schur(37, 1 << 31)[0][:1]]
     omegas = [nth_root_of_unity(37, p) for p in primes]
     assert _lib.schur_residues(37, primes, omegas)[1] == _lib.schur_residues(
         37, primes[1:], omegas[1:], method="glynn")[0]
     # the pinned residue of tests/test_cuda_device_schur_glynn.py:141-146
     assert _lib.schur_residues(33, [4294967161], [2662262]) == [1428739342]
+
+
+def test_wide_necklace_matches_glynn_cofactor_path(lib):
+    # odd moduli 2^30 <= p < 2^32 take the wide-modulus kernel (fully reduced
+    # sums, 33-bit Montgomery step); the Glynn minor runs them through the
+    # 32-bit (p < 2^31) and 64-bit (p >= 2^31) residue kernels
+    from permgpu import _lib
+    from permgpu.crt import nth_root_of_unity, plan_schur
+    n = 37
+    wide = plan_schur(n, 1 << 31)[0][:2] + plan_schur(n, 1 << 32)[0][:1]
+    assert all(p >= 1 << 30 for p in wide) and wide[-1] > 1 << 31
+    narrow = plan_schur(n)[0][:1]
+    primes = narrow[:1] + wide[:1] + wide[1:]
+    omegas = [nth_root_of_unity(n, p) for p in primes]
+    a = _lib.schur_residues(n, primes, omegas, method="necklace")
+    b = _lib.schur_residues(n, primes, omegas, method="glynn")
+    assert a == b
+    # narrow and wide moduli in one call come back in call order
+    assert a[:1] == _lib.schur_residues(n, primes[:1], omegas[:1], method="necklace")
+    assert a[1:] == _lib.schur_residues(n, primes[1:], omegas[1:], method="necklace")
+
+
+@pytest.mark.parametrize("n", [41, 47])
+def test_reference_gpu_residue_pins_through_wide_necklace(lib, n):
+    # the reference's CUDA residues at 32-bit pseudo-Mersenne primes
+    # (tests/test_cuda_device_schur_glynn.py:153-172), computed on the GPU
+    from permgpu import _lib
+    pins = [c for c in json.loads((GOLDEN / "schur.json").read_text())["pins"] if c["n"] == n]
+    assert pins
+    for pin in pins:
+        assert _lib.schur_residues(n, [pin["p"]], [pin["omega"]]) == [pin["residue"]]

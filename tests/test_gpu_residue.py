@@ -111,10 +111,8 @@ def test_schur_golden_residues_and_pin(lib):
     s = golden("schur.json")
     for c in s["residues"]:
         assert lib.schur_residues(c["n"], [c["p"]], [c["omega"]])[0] == c["residue"], c
-    # the n = 41 / 47 pins use 32-bit primes, which only the 64-bit Glynn
-    # kernel takes (2^39 / 2^45 states): they are checked against the table
-    # on the CPU, and the exact perm(S_41), perm(S_43) through the necklace
-    # kernel in test_gpu_necklace.py
+    # the n = 41 / 47 pins (32-bit primes) run through the wide-modulus
+    # necklace kernel in test_gpu_necklace.py
     for pin in s["pins"]:
         if pin["n"] <= 33:
             assert lib.schur_residues(pin["n"], [pin["p"]], [pin["omega"]])[0] == pin["residue"]

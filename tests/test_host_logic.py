@@ -167,6 +167,10 @@ def test_schur_necklace_method_rejects_unsupported_inputs():
     with pytest.raises(_lib.PermGpuError, match="PG_ERANGE"):
         _lib.schur_residues(11, [2147483629], [1], method="necklace")          # p >= 2^30
     with pytest.raises(_lib.PermGpuError, match="PG_ERANGE"):
+        _lib.schur_residues(29, [2147483629], [1], method="necklace")          # no wide kernel
+    with pytest.raises(_lib.PermGpuError, match="PG_ERANGE"):
+        _lib.schur_residues(41, [4294967311], [1], method="necklace")          # p >= 2^32
+    with pytest.raises(_lib.PermGpuError, match="PG_ERANGE"):
         _lib.schur_residues(11, [23], [5], method="necklace")                  # 5^11 != 1 mod 23
     with pytest.raises(ValueError):
         _lib.schur_residues(11, [23], [1], method="ryser")
