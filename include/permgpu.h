@@ -56,8 +56,9 @@ void pg_clear_abort(void);
  *           each modulus on the host exactly as perm_c_omp.c:911 does)
  *   n       0 <= n < 64
  *   moduli  1 <= m < 2^63, any parity (odd m < 2^31 run the 32-bit
- *           Montgomery Glynn kernel; odd m >= 2^31 the 64-bit one; even m
- *           split as 2^e * odd with a wrap-around Ryser kernel for 2^e)
+ *           Montgomery Glynn kernel; odd m < 2^32 its fully reduced wide
+ *           form; larger odd m the 64-bit one; even m split as 2^e * odd
+ *           with a wrap-around Ryser kernel for 2^e)
  * Replaces perm_c_ext.permanent_mod_p / ryser_permanent_mod_p
  * (perm_c_omp.c:858-937, dispatch :846-854) and permanent_modp_cuda
  * (perm_modp_cuda.cu:740-868).  All odd moduli below 2^31 share one launch.

@@ -47,6 +47,26 @@ __device__ __forceinline__ uint32_t m32_redc_mul(uint32_t a, uint32_t b,
     return (uint32_t)(u >> 32);
 }
 
+// Wide moduli 2^31 <= p < 2^32 (the 2^32 - c primes): values are kept fully
+// reduced in [0, p) and intermediate sums take 33 bits.
+// (a + b) mod p for a, b < p < 2^32
+__device__ __forceinline__ uint32_t m32w_addmod(uint32_t a, uint32_t b, uint32_t p) {
+    const uint64_t s = (uint64_t)a + b;
+    return s >= p ? (uint32_t)(s - p) : (uint32_t)s;
+}
+
+// a * b * 2^-32 mod p for a, b < p < 2^32, fully reduced.  With
+// m = -t p^-1 mod 2^32 the low words of t and m*p add to 0 or exactly 2^32
+// (a carry iff lo(t) != 0), and (t + m*p) / 2^32 < 2p needs 33 bits.
+__device__ __forceinline__ uint32_t m32w_redc_mul(uint32_t a, uint32_t b, uint32_t p,
+                                                  uint32_t pinv) {
+    const uint64_t t = (uint64_t)a * b;
+    const uint32_t m = (uint32_t)t * pinv;
+    const uint64_t mp = (uint64_t)m * p;
+    const uint64_t u = (t >> 32) + (mp >> 32) + ((uint32_t)t != 0u);
+    return u >= p ? (uint32_t)(u - p) : (uint32_t)u;
+}
+
 __device__ __forceinline__ constexpr int ctz_small(int r) {
     return (r & 1) ? 0 : (r & 2) ? 1 : (r & 4) ? 2 : (r & 8) ? 3 : 4;
 }
@@ -65,7 +85,9 @@ __host__ __device__ constexpr int m32_min_blocks(int N) {
            : (65536 / (256 * (N + 40)));
 }
 
-template <int N>
+// W: wide moduli (2^31 <= p < 2^32).  The tables then hold the plain
+// residues of +2a and -2a, sums and products stay fully reduced.
+template <int N, bool W = false>
 __global__ void __launch_bounds__(256, m32_min_blocks(N))
 glynn_m32_kernel(M32Args a) {
     constexpr int NP = (N + 3) & ~3;
@@ -108,7 +130,8 @@ glynn_m32_kernel(M32Args a) {
             if ((gstart >> j) & 1) {
                 const uint32_t *col = tab + (2 * j + 1) * NP;
 #pragma unroll
-                for (int i = 0; i < N; i++) s[i] = m32_addmod(s[i], col[i], p);
+                for (int i = 0; i < N; i++)
+                    s[i] = W ? m32w_addmod(s[i], col[i], p) : m32_addmod(s[i], col[i], p);
             }
         }
     }
@@ -141,31 +164,41 @@ glynn_m32_kernel(M32Args a) {
                 if (step) {
                     const uint4 *col =
                         reinterpret_cast<const uint4 *>(tab + (2 * j + sub) * NP);
+                    const auto add = [&](uint32_t x, uint32_t d) {
+                        return W ? m32w_addmod(x, d, p) : m32_addmod(x, d, p);
+                    };
 #pragma unroll
                     for (int v = 0; v < NP / 4; v++) {
                         const uint4 d = col[v];
-                        if (4 * v + 0 < N) s[4 * v + 0] = m32_addmod(s[4 * v + 0], d.x, p);
-                        if (4 * v + 1 < N) s[4 * v + 1] = m32_addmod(s[4 * v + 1], d.y, p);
-                        if (4 * v + 2 < N) s[4 * v + 2] = m32_addmod(s[4 * v + 2], d.z, p);
-                        if (4 * v + 3 < N) s[4 * v + 3] = m32_addmod(s[4 * v + 3], d.w, p);
+                        if (4 * v + 0 < N) s[4 * v + 0] = add(s[4 * v + 0], d.x);
+                        if (4 * v + 1 < N) s[4 * v + 1] = add(s[4 * v + 1], d.y);
+                        if (4 * v + 2 < N) s[4 * v + 2] = add(s[4 * v + 2], d.z);
+                        if (4 * v + 3 < N) s[4 * v + 3] = add(s[4 * v + 3], d.w);
                     }
                 }
                 // NCH independent REDC chains over interleaved rows, then a
                 // combining tree; each combine first brings one side below p.
                 constexpr int NCH = N >= 16 ? 4 : (N >= 4 ? 2 : 1);
+                // narrow: chains below 2p, one side of each combine brought
+                // below p; wide: everything fully reduced
+                const auto mul = [&](uint32_t x, uint32_t y) {
+                    return W ? m32w_redc_mul(x, y, p, pinv) : m32_redc_mul(x, y, p, pinv);
+                };
+                const auto low = [&](uint32_t x) {
+                    return W ? x : __viaddmin_u32(x, 0u - p, x);
+                };
                 uint32_t ch[NCH];
 #pragma unroll
                 for (int t = 0; t < NCH; t++) ch[t] = s[t];
 #pragma unroll
-                for (int i = NCH; i < N; i++)
-                    ch[i % NCH] = m32_redc_mul(ch[i % NCH], s[i], p, pinv);
+                for (int i = NCH; i < N; i++) ch[i % NCH] = mul(ch[i % NCH], s[i]);
                 uint32_t prod;
                 if (NCH == 4) {
-                    const uint32_t c01 = m32_redc_mul(ch[0], __viaddmin_u32(ch[1], 0u - p, ch[1]), p, pinv);
-                    const uint32_t c23 = m32_redc_mul(ch[2], __viaddmin_u32(ch[3], 0u - p, ch[3]), p, pinv);
-                    prod = m32_redc_mul(c01, __viaddmin_u32(c23, 0u - p, c23), p, pinv);
+                    const uint32_t c01 = mul(ch[0], low(ch[1]));
+                    const uint32_t c23 = mul(ch[2], low(ch[3]));
+                    prod = mul(c01, low(c23));
                 } else if (NCH == 2) {
-                    prod = m32_redc_mul(ch[0], __viaddmin_u32(ch[1], 0u - p, ch[1]), p, pinv);
+                    prod = mul(ch[0], low(ch[1]));
                 } else {
                     prod = ch[0];
                 }
@@ -178,7 +211,7 @@ glynn_m32_kernel(M32Args a) {
         thread_sum += e >= o ? e - o : e + (p - o);
     }
 
-    // block reduction of the per-thread residues (< 2^31 each after the
+    // block reduction of the per-thread residues (< 2^32 each after the
     // fold, so the 64-bit atomic sum over all blocks cannot overflow)
     thread_sum %= p;
     __shared__ unsigned long long red[8];
@@ -201,31 +234,31 @@ glynn_m32_kernel(M32Args a) {
 
 // Launch helper: grid (blocks_per_modulus, k), 256 threads, dynamic smem for
 // one modulus table.  Returns cudaError_t of the launch.
-template <int N>
+template <int N, bool W = false>
 cudaError_t launch_glynn_m32(const M32Args &args, int k, int blocks_per_mod,
                              cudaStream_t stream) {
     constexpr int NP = (N + 3) & ~3;
     const size_t smem = (size_t)(N - 1) * 2 * NP * sizeof(uint32_t);
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(
-            glynn_m32_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            glynn_m32_kernel<N, W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
             (int)smem);
         if (e != cudaSuccess) return e;
     }
     dim3 grid(blocks_per_mod, k);
-    glynn_m32_kernel<N><<<grid, 256, smem, stream>>>(args);
+    glynn_m32_kernel<N, W><<<grid, 256, smem, stream>>>(args);
     return cudaGetLastError();
 }
 
-template <int N>
+template <int N, bool W = false>
 int occupancy_glynn_m32() {
     constexpr int NP = (N + 3) & ~3;
     const size_t smem = (size_t)(N - 1) * 2 * NP * sizeof(uint32_t);
     if (smem > 48 * 1024)
-        cudaFuncSetAttribute(glynn_m32_kernel<N>,
+        cudaFuncSetAttribute(glynn_m32_kernel<N, W>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, glynn_m32_kernel<N>, 256,
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, glynn_m32_kernel<N, W>, 256,
                                                       smem) != cudaSuccess)
         return 1;
     return nb < 1 ? 1 : nb;
@@ -241,5 +274,15 @@ cudaError_t launch_glynn_m32_hi(int N, const M32Args &args, int k,
 int occupancy_glynn_m32_lo(int N);
 int occupancy_glynn_m32_mid(int N);
 int occupancy_glynn_m32_hi(int N);
+// The same for wide moduli (glynn_m32w_*.cu).
+cudaError_t launch_glynn_m32w_lo(int N, const M32Args &args, int k,
+                                 int blocks_per_mod, cudaStream_t stream);
+cudaError_t launch_glynn_m32w_mid(int N, const M32Args &args, int k,
+                                  int blocks_per_mod, cudaStream_t stream);
+cudaError_t launch_glynn_m32w_hi(int N, const M32Args &args, int k,
+                                 int blocks_per_mod, cudaStream_t stream);
+int occupancy_glynn_m32w_lo(int N);
+int occupancy_glynn_m32w_mid(int N);
+int occupancy_glynn_m32w_hi(int N);
 
 }  // namespace pg

@@ -337,26 +337,9 @@ __host__ __device__ constexpr int nk_stride(int L) {
 // below p (< 2p), and the Montgomery chain stays below 2p as long as
 // 4p < 2^32: NECKLACE_PRIME_LIMIT = 2^30.  The wide form (W) takes odd
 // moduli up to 2^32 (the reference's 32-bit pseudo-Mersenne primes) and
-// keeps every value fully reduced, with 33-bit intermediate sums.
+// keeps every value fully reduced, with 33-bit intermediate sums
+// (m32w_addmod, m32w_redc_mul).
 constexpr uint64_t NK_PRIME_LIMIT = NECKLACE_PRIME_LIMIT;
-
-// (a + b) mod p for a, b < p < 2^32
-__device__ __forceinline__ uint32_t nk_addmod_w(uint32_t a, uint32_t b, uint32_t p) {
-    const uint64_t s = (uint64_t)a + b;
-    return s >= p ? (uint32_t)(s - p) : (uint32_t)s;
-}
-
-// a * b * 2^-32 mod p for a, b < p < 2^32, fully reduced.  With
-// m = -t p^-1 mod 2^32 the low words of t and m*p add to 0 or exactly 2^32
-// (a carry iff lo(t) != 0), and (t + m*p) / 2^32 < 2p needs 33 bits.
-__device__ __forceinline__ uint32_t nk_redc_w(uint32_t a, uint32_t b, uint32_t p,
-                                              uint32_t pinv) {
-    const uint64_t t = (uint64_t)a * b;
-    const uint32_t m = (uint32_t)t * pinv;
-    const uint64_t mp = (uint64_t)m * p;
-    const uint64_t u = (t >> 32) + (mp >> 32) + ((uint32_t)t != 0u);
-    return u >= p ? (uint32_t)(u - p) : (uint32_t)u;
-}
 
 struct NeckArgs {
     // [k][256][LS]: entry (v, x) = sum over set bits t of the byte v of
@@ -404,7 +387,7 @@ struct NeckLane {
 #pragma unroll
             for (int r = 0; r < L; r++) {
                 const uint32_t d = t[(r + 8 * j) % L];
-                hm[r] = W ? nk_addmod_w(hm[r], d, p) : m32_addmod(hm[r], d - p, p);
+                hm[r] = W ? m32w_addmod(hm[r], d, p) : m32_addmod(hm[r], d - p, p);
             }
         }
         cur = 0;
@@ -425,7 +408,7 @@ struct NeckLane {
             for (int r = 0; r < L; r++) {
                 const uint32_t x = tn[(r + 8 * j) % L], y = to[(r + 8 * j) % L];
                 const uint32_t d = x >= y ? x - y : x - y + p;     // (x - y) mod p
-                hm[r] = W ? nk_addmod_w(hm[r], d, p) : m32_addmod(hm[r], d - p, p);
+                hm[r] = W ? m32w_addmod(hm[r], d, p) : m32_addmod(hm[r], d - p, p);
             }
         }
         cur = nw;
@@ -438,10 +421,10 @@ struct NeckLane {
         // narrow: lazy sums below 2p and the chain of the residue kernel;
         // wide: fully reduced sums and products
         const auto add2 = [&](uint32_t x, uint32_t y) {
-            return W ? nk_addmod_w(x, y, p) : x + y;
+            return W ? m32w_addmod(x, y, p) : x + y;
         };
         const auto mul = [&](uint32_t x, uint32_t y) {
-            return W ? nk_redc_w(x, y, p, pinv) : m32_redc_mul(x, y, p, pinv);
+            return W ? m32w_redc_mul(x, y, p, pinv) : m32_redc_mul(x, y, p, pinv);
         };
         uint32_t prod;
         if constexpr (L >= 8) {

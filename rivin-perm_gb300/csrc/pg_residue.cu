@@ -1,7 +1,8 @@
 // Residue engine host logic and the wide-modulus kernels.
 //
 //  * odd m < 2^31   -> glynn_m32_kernel<N> (all such moduli in one launch)
-//  * odd m >= 2^31  -> glynn_m64_kernel (64-bit Montgomery, runtime n)
+//  * odd m < 2^32   -> glynn_m32_kernel<N, true> (fully reduced, 33-bit sums)
+//  * odd m >= 2^32  -> glynn_m64_kernel (64-bit Montgomery, runtime n)
 //  * even m = 2^e*o -> odd part as above, 2^e part from ryser_wrap64_kernel
 //                      (Ryser in Z/2^64), recombined by CRT on the host
 //
@@ -128,13 +129,23 @@ __global__ void ryser_wrap64_kernel(RyserArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-static cudaError_t launch_m32_any(int N, const M32Args &args, int k, int bpm,
+static cudaError_t launch_m32_any(int N, bool wide, const M32Args &args, int k, int bpm,
                                   cudaStream_t st) {
+    if (wide) {
+        if (N <= 22) return launch_glynn_m32w_lo(N, args, k, bpm, st);
+        if (N <= 42) return launch_glynn_m32w_mid(N, args, k, bpm, st);
+        return launch_glynn_m32w_hi(N, args, k, bpm, st);
+    }
     if (N <= 22) return launch_glynn_m32_lo(N, args, k, bpm, st);
     if (N <= 42) return launch_glynn_m32_mid(N, args, k, bpm, st);
     return launch_glynn_m32_hi(N, args, k, bpm, st);
 }
-static int occupancy_m32_any(int N) {
+static int occupancy_m32_any(int N, bool wide) {
+    if (wide) {
+        if (N <= 22) return occupancy_glynn_m32w_lo(N);
+        if (N <= 42) return occupancy_glynn_m32w_mid(N);
+        return occupancy_glynn_m32w_hi(N);
+    }
     if (N <= 22) return occupancy_glynn_m32_lo(N);
     if (N <= 42) return occupancy_glynn_m32_mid(N);
     return occupancy_glynn_m32_hi(N);
@@ -142,13 +153,15 @@ static int occupancy_m32_any(int N) {
 
 static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
-// per(mats[t]) mod moduli[t] for odd moduli 3 <= m < 2^31, n >= 2.
+// per(mats[t]) mod moduli[t] for odd moduli 3 <= m < 2^31, or for odd
+// 2^31 <= m < 2^32 with `wide` (fully reduced form of the same kernel), n >= 2.
 static int glynn_m32_batch(const uint64_t *mats, int n, const uint64_t *moduli,
-                           int k, uint64_t *out) {
+                           int k, bool wide, uint64_t *out) {
     if (k > 65535) {   // grid.y limit: split into launches of <= 65535 moduli
         for (int t0 = 0; t0 < k; t0 += 65535) {
             const int kk = k - t0 < 65535 ? k - t0 : 65535;
-            int st = glynn_m32_batch(mats + (size_t)t0 * n * n, n, moduli + t0, kk, out + t0);
+            int st = glynn_m32_batch(mats + (size_t)t0 * n * n, n, moduli + t0, kk, wide,
+                                     out + t0);
             if (st != PG_OK) return st;
         }
         return PG_OK;
@@ -190,8 +203,13 @@ static int glynn_m32_batch(const uint64_t *mats, int n, const uint64_t *moduli,
         for (int j = 0; j < NCOL; j++) {
             for (int i = 0; i < N; i++) {
                 const uint32_t two = (uint32_t)((2 * m[i * n + j]) % p);
-                tt[(2 * j + 0) * NP + i] = two - p;   // add: (s + two) mod p
-                tt[(2 * j + 1) * NP + i] = 0u - two;  // sub: (s - two) mod p
+                if (wide) {
+                    tt[(2 * j + 0) * NP + i] = two;                // add
+                    tt[(2 * j + 1) * NP + i] = two ? p - two : 0;  // sub
+                } else {
+                    tt[(2 * j + 0) * NP + i] = two - p;   // add: (s + two) mod p
+                    tt[(2 * j + 1) * NP + i] = 0u - two;  // sub: (s - two) mod p
+                }
             }
         }
         for (int i = 0; i < N; i++) {
@@ -204,7 +222,7 @@ static int glynn_m32_batch(const uint64_t *mats, int n, const uint64_t *moduli,
     // Launch shape: one resident wave of blocks shared by the k moduli; each
     // thread owns a contiguous range of ~128 chunks of >= 64 states (small
     // orders use fewer blocks so every thread keeps >= 512 states).
-    const int occ = occupancy_m32_any(N);
+    const int occ = occupancy_m32_any(N, wide);
     const int log_states = n - 1;
     uint64_t bpm = ((uint64_t)occ * dev.sm_count + k - 1) / k;
     while (bpm > 1 && ((1ull << log_states) >> 9) < bpm * 256) bpm >>= 1;
@@ -233,7 +251,7 @@ static int glynn_m32_batch(const uint64_t *mats, int n, const uint64_t *moduli,
 
     PG_CUDA(cudaMemcpyAsync(d, h, off_acc, cudaMemcpyHostToDevice, ws->stream));
     PG_CUDA(cudaMemsetAsync(d + off_acc, 0, total - off_acc, ws->stream));
-    PG_CUDA(launch_m32_any(N, args, k, (int)bpm, ws->stream));
+    PG_CUDA(launch_m32_any(N, wide, args, k, (int)bpm, ws->stream));
     PG_CUDA(cudaMemcpyAsync(h + off_acc, d + off_acc, total - off_acc,
                             cudaMemcpyDeviceToHost, ws->stream));
     PG_CUDA(cudaStreamSynchronize(ws->stream));
@@ -318,20 +336,23 @@ static int glynn_m64_batch(const uint64_t *mats, int n, const uint64_t *moduli,
 
 int glynn_residues_odd(const uint64_t *mats, int n, const uint64_t *moduli,
                        int k, uint64_t *out) {
-    // n >= 2, every modulus odd and >= 3.
-    std::vector<int> small, wide;
-    for (int t = 0; t < k; t++) (moduli[t] < (1ull << 31) ? small : wide).push_back(t);
+    // n >= 2, every modulus odd and >= 3: m < 2^31 narrow 32-bit kernel,
+    // m < 2^32 its wide form, larger moduli the 64-bit kernel
+    std::vector<int> cls[3];
+    for (int t = 0; t < k; t++)
+        cls[moduli[t] < (1ull << 31) ? 0 : moduli[t] < (1ull << 32) ? 1 : 2].push_back(t);
     const size_t nn = (size_t)n * n;
-    for (int pass = 0; pass < 2; pass++) {
-        const std::vector<int> &idx = pass == 0 ? small : wide;
+    for (int pass = 0; pass < 3; pass++) {
+        const std::vector<int> &idx = cls[pass];
         if (idx.empty()) continue;
         std::vector<uint64_t> m(idx.size() * nn), mod(idx.size()), res(idx.size());
         for (size_t q = 0; q < idx.size(); q++) {
             std::memcpy(&m[q * nn], mats + idx[q] * nn, nn * 8);
             mod[q] = moduli[idx[q]];
         }
-        int st = pass == 0
-                     ? glynn_m32_batch(m.data(), n, mod.data(), (int)idx.size(), res.data())
+        int st = pass < 2
+                     ? glynn_m32_batch(m.data(), n, mod.data(), (int)idx.size(), pass == 1,
+                                       res.data())
                      : glynn_m64_batch(m.data(), n, mod.data(), (int)idx.size(), res.data());
         if (st != PG_OK) return st;
         for (size_t q = 0; q < idx.size(); q++) out[idx[q]] = res[q];

@@ -49,6 +49,33 @@ def test_exhaustive_signed_order_two(lib):
             [_definition(m) % p for p in mods]
 
 
+# odd moduli 2^31 <= m < 2^32 take the wide form of the 32-bit kernel:
+# primes just above 2^31, 3037000501, the largest 32-bit prime, the
+# reference's pseudo-Mersenne Schur primes and an odd composite
+WIDE_MODULI = [2_147_483_659, 3_037_000_501, 4_294_966_153, 4_294_967_161,
+               4_294_967_291, 4_294_967_295]
+
+
+@pytest.mark.parametrize("n", [2, 3, 4, 5, 9, 16, 17, 22, 23])
+def test_wide_32bit_moduli_against_oracle(lib, n):
+    rng = np.random.default_rng(2000 + n)
+    a = rng.integers(-(1 << 40), 1 << 40, (n, n), dtype=np.int64)
+    want = [oracle.permanent_mod_p(a, p, 8) for p in WIDE_MODULI]
+    assert lib.residues(a, WIDE_MODULI) == want
+    # mixed with narrow and 64-bit moduli in one call, results in call order
+    mods = [1_000_003] + WIDE_MODULI[:2] + [(1 << 61) - 1, 4_294_967_311]
+    assert lib.residues(a, mods) == [oracle.permanent_mod_p(a, p, 8) for p in mods]
+
+
+@pytest.mark.parametrize("n", [30, 34])
+def test_wide_32bit_moduli_large_orders_against_exact(lib, n):
+    # full-size property: residues equal the exact engine's integer mod m
+    rng = np.random.default_rng(3000 + n)
+    a = rng.integers(-2, 3, (n, n), dtype=np.int64)
+    exact = lib.exact_permanent(a, 12)
+    assert lib.residues(a, WIDE_MODULI) == [exact % p for p in WIDE_MODULI]
+
+
 @pytest.mark.parametrize("n", list(range(2, 24)))
 def test_every_small_order_against_oracle(lib, n):
     rng = np.random.default_rng(1000 + n)
