@@ -363,6 +363,9 @@ int occupancy_exact_glynn() {
     return nb < 1 ? 1 : nb;
 }
 
+// Largest compiled group size (gen_exact_inst.py); hosts try G from here down.
+constexpr int EXACT_MAX_G = 10;
+
 // Compiled (N, G) pairs; returns cudaErrorInvalidValue / 0 when absent.
 cudaError_t launch_exact_any(int N, int G, const ExactArgs &args, int blocks,
                              cudaStream_t stream);

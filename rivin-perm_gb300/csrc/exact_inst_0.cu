@@ -1,108 +1,102 @@
-// Instantiations of the exact Glynn kernel (part 0 of 8).
+// Instantiations of the exact Glynn kernel (part 0 of 12),
+// written by gen_exact_inst.py.
 #include "exact_glynn.cuh"
 
 namespace pg {
 
 bool exact_dispatch_0(int N, int G, const ExactArgs *args, int blocks,
                        cudaStream_t stream, cudaError_t *err, int *occ) {
-    switch (N * 8 + G) {
-    case 17:
+    switch (N * 16 + G) {
+    case 33:
         if (args) *err = launch_exact_glynn<2, 1>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<2, 1>();
         return true;
-    case 36:
-        if (args) *err = launch_exact_glynn<4, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<4, 4>();
+    case 84:
+        if (args) *err = launch_exact_glynn<5, 4>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<5, 4>();
         return true;
-    case 52:
-        if (args) *err = launch_exact_glynn<6, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<6, 4>();
-        return true;
-    case 68:
+    case 132:
         if (args) *err = launch_exact_glynn<8, 4>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<8, 4>();
         return true;
-    case 84:
-        if (args) *err = launch_exact_glynn<10, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<10, 4>();
+    case 180:
+        if (args) *err = launch_exact_glynn<11, 4>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<11, 4>();
         return true;
-    case 100:
-        if (args) *err = launch_exact_glynn<12, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<12, 4>();
-        return true;
-    case 116:
+    case 228:
         if (args) *err = launch_exact_glynn<14, 4>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<14, 4>();
         return true;
-    case 132:
-        if (args) *err = launch_exact_glynn<16, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<16, 4>();
+    case 290:
+        if (args) *err = launch_exact_glynn<18, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<18, 2>();
         return true;
-    case 155:
-        if (args) *err = launch_exact_glynn<19, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<19, 3>();
-        return true;
-    case 178:
+    case 354:
         if (args) *err = launch_exact_glynn<22, 2>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<22, 2>();
         return true;
-    case 196:
-        if (args) *err = launch_exact_glynn<24, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<24, 4>();
+    case 392:
+        if (args) *err = launch_exact_glynn<24, 8>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<24, 8>();
         return true;
-    case 210:
-        if (args) *err = launch_exact_glynn<26, 2>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<26, 2>();
+    case 420:
+        if (args) *err = launch_exact_glynn<26, 4>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<26, 4>();
         return true;
-    case 221:
-        if (args) *err = launch_exact_glynn<27, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<27, 5>();
+    case 440:
+        if (args) *err = launch_exact_glynn<27, 8>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<27, 8>();
         return true;
-    case 235:
-        if (args) *err = launch_exact_glynn<29, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<29, 3>();
+    case 468:
+        if (args) *err = launch_exact_glynn<29, 4>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<29, 4>();
         return true;
-    case 246:
-        if (args) *err = launch_exact_glynn<30, 6>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<30, 6>();
+    case 488:
+        if (args) *err = launch_exact_glynn<30, 8>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<30, 8>();
         return true;
-    case 260:
+    case 516:
         if (args) *err = launch_exact_glynn<32, 4>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<32, 4>();
         return true;
-    case 276:
-        if (args) *err = launch_exact_glynn<34, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<34, 4>();
+    case 538:
+        if (args) *err = launch_exact_glynn<33, 10>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<33, 10>();
         return true;
-    case 292:
-        if (args) *err = launch_exact_glynn<36, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<36, 4>();
+    case 567:
+        if (args) *err = launch_exact_glynn<35, 7>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<35, 7>();
         return true;
-    case 308:
-        if (args) *err = launch_exact_glynn<38, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<38, 4>();
+    case 597:
+        if (args) *err = launch_exact_glynn<37, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<37, 5>();
         return true;
-    case 324:
-        if (args) *err = launch_exact_glynn<40, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<40, 4>();
+    case 627:
+        if (args) *err = launch_exact_glynn<39, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<39, 3>();
         return true;
-    case 340:
-        if (args) *err = launch_exact_glynn<42, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<42, 4>();
+    case 648:
+        if (args) *err = launch_exact_glynn<40, 8>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<40, 8>();
         return true;
-    case 356:
+    case 678:
+        if (args) *err = launch_exact_glynn<42, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<42, 6>();
+        return true;
+    case 708:
         if (args) *err = launch_exact_glynn<44, 4>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<44, 4>();
         return true;
-    case 372:
-        if (args) *err = launch_exact_glynn<46, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<46, 4>();
+    case 730:
+        if (args) *err = launch_exact_glynn<45, 10>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<45, 10>();
         return true;
-    case 388:
-        if (args) *err = launch_exact_glynn<48, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<48, 4>();
+    case 759:
+        if (args) *err = launch_exact_glynn<47, 7>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<47, 7>();
         return true;
-    default: return false;
+    default:
+        return false;
     }
 }
 

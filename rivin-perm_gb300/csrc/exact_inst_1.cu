@@ -1,108 +1,102 @@
-// Instantiations of the exact Glynn kernel (part 1 of 8).
+// Instantiations of the exact Glynn kernel (part 1 of 12),
+// written by gen_exact_inst.py.
 #include "exact_glynn.cuh"
 
 namespace pg {
 
 bool exact_dispatch_1(int N, int G, const ExactArgs *args, int blocks,
                        cudaStream_t stream, cudaError_t *err, int *occ) {
-    switch (N * 8 + G) {
-    case 18:
+    switch (N * 16 + G) {
+    case 34:
         if (args) *err = launch_exact_glynn<2, 2>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<2, 2>();
         return true;
-    case 41:
-        if (args) *err = launch_exact_glynn<5, 1>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<5, 1>();
+    case 97:
+        if (args) *err = launch_exact_glynn<6, 1>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<6, 1>();
         return true;
-    case 57:
-        if (args) *err = launch_exact_glynn<7, 1>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<7, 1>();
-        return true;
-    case 73:
+    case 145:
         if (args) *err = launch_exact_glynn<9, 1>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<9, 1>();
         return true;
-    case 89:
-        if (args) *err = launch_exact_glynn<11, 1>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<11, 1>();
+    case 193:
+        if (args) *err = launch_exact_glynn<12, 1>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<12, 1>();
         return true;
-    case 105:
-        if (args) *err = launch_exact_glynn<13, 1>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<13, 1>();
-        return true;
-    case 121:
+    case 241:
         if (args) *err = launch_exact_glynn<15, 1>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<15, 1>();
         return true;
-    case 138:
-        if (args) *err = launch_exact_glynn<17, 2>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<17, 2>();
+    case 291:
+        if (args) *err = launch_exact_glynn<18, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<18, 3>();
         return true;
-    case 156:
-        if (args) *err = launch_exact_glynn<19, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<19, 4>();
-        return true;
-    case 179:
+    case 355:
         if (args) *err = launch_exact_glynn<22, 3>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<22, 3>();
         return true;
-    case 197:
-        if (args) *err = launch_exact_glynn<24, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<24, 5>();
+    case 394:
+        if (args) *err = launch_exact_glynn<24, 10>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<24, 10>();
         return true;
-    case 211:
-        if (args) *err = launch_exact_glynn<26, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<26, 3>();
+    case 421:
+        if (args) *err = launch_exact_glynn<26, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<26, 5>();
         return true;
-    case 222:
-        if (args) *err = launch_exact_glynn<27, 6>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<27, 6>();
+    case 442:
+        if (args) *err = launch_exact_glynn<27, 10>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<27, 10>();
         return true;
-    case 236:
-        if (args) *err = launch_exact_glynn<29, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<29, 4>();
+    case 469:
+        if (args) *err = launch_exact_glynn<29, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<29, 5>();
         return true;
-    case 250:
-        if (args) *err = launch_exact_glynn<31, 2>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<31, 2>();
+    case 490:
+        if (args) *err = launch_exact_glynn<30, 10>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<30, 10>();
         return true;
-    case 261:
+    case 517:
         if (args) *err = launch_exact_glynn<32, 5>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<32, 5>();
         return true;
-    case 277:
-        if (args) *err = launch_exact_glynn<34, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<34, 5>();
+    case 547:
+        if (args) *err = launch_exact_glynn<34, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<34, 3>();
         return true;
-    case 293:
-        if (args) *err = launch_exact_glynn<36, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<36, 5>();
+    case 568:
+        if (args) *err = launch_exact_glynn<35, 8>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<35, 8>();
         return true;
-    case 309:
-        if (args) *err = launch_exact_glynn<38, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<38, 5>();
+    case 598:
+        if (args) *err = launch_exact_glynn<37, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<37, 6>();
         return true;
-    case 325:
-        if (args) *err = launch_exact_glynn<40, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<40, 5>();
+    case 628:
+        if (args) *err = launch_exact_glynn<39, 4>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<39, 4>();
         return true;
-    case 341:
-        if (args) *err = launch_exact_glynn<42, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<42, 5>();
+    case 650:
+        if (args) *err = launch_exact_glynn<40, 10>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<40, 10>();
         return true;
-    case 357:
+    case 679:
+        if (args) *err = launch_exact_glynn<42, 7>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<42, 7>();
+        return true;
+    case 709:
         if (args) *err = launch_exact_glynn<44, 5>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<44, 5>();
         return true;
-    case 373:
-        if (args) *err = launch_exact_glynn<46, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<46, 5>();
+    case 739:
+        if (args) *err = launch_exact_glynn<46, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<46, 3>();
         return true;
-    case 389:
-        if (args) *err = launch_exact_glynn<48, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<48, 5>();
+    case 760:
+        if (args) *err = launch_exact_glynn<47, 8>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<47, 8>();
         return true;
-    default: return false;
+    default:
+        return false;
     }
 }
 

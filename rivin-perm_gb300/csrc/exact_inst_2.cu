@@ -1,108 +1,102 @@
-// Instantiations of the exact Glynn kernel (part 2 of 8).
+// Instantiations of the exact Glynn kernel (part 2 of 12),
+// written by gen_exact_inst.py.
 #include "exact_glynn.cuh"
 
 namespace pg {
 
 bool exact_dispatch_2(int N, int G, const ExactArgs *args, int blocks,
                        cudaStream_t stream, cudaError_t *err, int *occ) {
-    switch (N * 8 + G) {
-    case 25:
+    switch (N * 16 + G) {
+    case 49:
         if (args) *err = launch_exact_glynn<3, 1>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<3, 1>();
         return true;
-    case 42:
-        if (args) *err = launch_exact_glynn<5, 2>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<5, 2>();
+    case 98:
+        if (args) *err = launch_exact_glynn<6, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<6, 2>();
         return true;
-    case 58:
-        if (args) *err = launch_exact_glynn<7, 2>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<7, 2>();
-        return true;
-    case 74:
+    case 146:
         if (args) *err = launch_exact_glynn<9, 2>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<9, 2>();
         return true;
-    case 90:
-        if (args) *err = launch_exact_glynn<11, 2>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<11, 2>();
+    case 194:
+        if (args) *err = launch_exact_glynn<12, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<12, 2>();
         return true;
-    case 106:
-        if (args) *err = launch_exact_glynn<13, 2>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<13, 2>();
-        return true;
-    case 122:
+    case 242:
         if (args) *err = launch_exact_glynn<15, 2>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<15, 2>();
         return true;
-    case 139:
-        if (args) *err = launch_exact_glynn<17, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<17, 3>();
+    case 292:
+        if (args) *err = launch_exact_glynn<18, 4>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<18, 4>();
         return true;
-    case 162:
-        if (args) *err = launch_exact_glynn<20, 2>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<20, 2>();
-        return true;
-    case 180:
+    case 356:
         if (args) *err = launch_exact_glynn<22, 4>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<22, 4>();
         return true;
-    case 198:
-        if (args) *err = launch_exact_glynn<24, 6>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<24, 6>();
+    case 402:
+        if (args) *err = launch_exact_glynn<25, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<25, 2>();
         return true;
-    case 212:
-        if (args) *err = launch_exact_glynn<26, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<26, 4>();
+    case 422:
+        if (args) *err = launch_exact_glynn<26, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<26, 6>();
         return true;
-    case 226:
+    case 450:
         if (args) *err = launch_exact_glynn<28, 2>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<28, 2>();
         return true;
-    case 237:
-        if (args) *err = launch_exact_glynn<29, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<29, 5>();
+    case 470:
+        if (args) *err = launch_exact_glynn<29, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<29, 6>();
         return true;
-    case 251:
-        if (args) *err = launch_exact_glynn<31, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<31, 3>();
+    case 498:
+        if (args) *err = launch_exact_glynn<31, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<31, 2>();
         return true;
-    case 262:
+    case 518:
         if (args) *err = launch_exact_glynn<32, 6>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<32, 6>();
         return true;
-    case 278:
-        if (args) *err = launch_exact_glynn<34, 6>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<34, 6>();
+    case 548:
+        if (args) *err = launch_exact_glynn<34, 4>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<34, 4>();
         return true;
-    case 294:
-        if (args) *err = launch_exact_glynn<36, 6>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<36, 6>();
+    case 570:
+        if (args) *err = launch_exact_glynn<35, 10>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<35, 10>();
         return true;
-    case 310:
-        if (args) *err = launch_exact_glynn<38, 6>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<38, 6>();
+    case 599:
+        if (args) *err = launch_exact_glynn<37, 7>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<37, 7>();
         return true;
-    case 326:
-        if (args) *err = launch_exact_glynn<40, 6>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<40, 6>();
+    case 629:
+        if (args) *err = launch_exact_glynn<39, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<39, 5>();
         return true;
-    case 342:
-        if (args) *err = launch_exact_glynn<42, 6>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<42, 6>();
+    case 659:
+        if (args) *err = launch_exact_glynn<41, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<41, 3>();
         return true;
-    case 358:
+    case 680:
+        if (args) *err = launch_exact_glynn<42, 8>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<42, 8>();
+        return true;
+    case 710:
         if (args) *err = launch_exact_glynn<44, 6>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<44, 6>();
         return true;
-    case 374:
-        if (args) *err = launch_exact_glynn<46, 6>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<46, 6>();
+    case 740:
+        if (args) *err = launch_exact_glynn<46, 4>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<46, 4>();
         return true;
-    case 390:
-        if (args) *err = launch_exact_glynn<48, 6>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<48, 6>();
+    case 762:
+        if (args) *err = launch_exact_glynn<47, 10>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<47, 10>();
         return true;
-    default: return false;
+    default:
+        return false;
     }
 }
 

@@ -1,104 +1,102 @@
-// Instantiations of the exact Glynn kernel (part 3 of 8).
+// Instantiations of the exact Glynn kernel (part 3 of 12),
+// written by gen_exact_inst.py.
 #include "exact_glynn.cuh"
 
 namespace pg {
 
 bool exact_dispatch_3(int N, int G, const ExactArgs *args, int blocks,
                        cudaStream_t stream, cudaError_t *err, int *occ) {
-    switch (N * 8 + G) {
-    case 26:
+    switch (N * 16 + G) {
+    case 50:
         if (args) *err = launch_exact_glynn<3, 2>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<3, 2>();
         return true;
-    case 43:
-        if (args) *err = launch_exact_glynn<5, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<5, 3>();
+    case 99:
+        if (args) *err = launch_exact_glynn<6, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<6, 3>();
         return true;
-    case 59:
-        if (args) *err = launch_exact_glynn<7, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<7, 3>();
-        return true;
-    case 75:
+    case 147:
         if (args) *err = launch_exact_glynn<9, 3>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<9, 3>();
         return true;
-    case 91:
-        if (args) *err = launch_exact_glynn<11, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<11, 3>();
+    case 195:
+        if (args) *err = launch_exact_glynn<12, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<12, 3>();
         return true;
-    case 107:
-        if (args) *err = launch_exact_glynn<13, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<13, 3>();
-        return true;
-    case 123:
+    case 243:
         if (args) *err = launch_exact_glynn<15, 3>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<15, 3>();
         return true;
-    case 140:
-        if (args) *err = launch_exact_glynn<17, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<17, 4>();
+    case 306:
+        if (args) *err = launch_exact_glynn<19, 2>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<19, 2>();
         return true;
-    case 163:
-        if (args) *err = launch_exact_glynn<20, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<20, 3>();
-        return true;
-    case 186:
+    case 370:
         if (args) *err = launch_exact_glynn<23, 2>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<23, 2>();
         return true;
-    case 202:
-        if (args) *err = launch_exact_glynn<25, 2>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<25, 2>();
+    case 403:
+        if (args) *err = launch_exact_glynn<25, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<25, 3>();
         return true;
-    case 213:
-        if (args) *err = launch_exact_glynn<26, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<26, 5>();
+    case 423:
+        if (args) *err = launch_exact_glynn<26, 7>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<26, 7>();
         return true;
-    case 227:
+    case 451:
         if (args) *err = launch_exact_glynn<28, 3>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<28, 3>();
         return true;
-    case 238:
-        if (args) *err = launch_exact_glynn<29, 6>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<29, 6>();
+    case 471:
+        if (args) *err = launch_exact_glynn<29, 7>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<29, 7>();
         return true;
-    case 252:
-        if (args) *err = launch_exact_glynn<31, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<31, 4>();
+    case 499:
+        if (args) *err = launch_exact_glynn<31, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<31, 3>();
         return true;
-    case 267:
-        if (args) *err = launch_exact_glynn<33, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<33, 3>();
+    case 519:
+        if (args) *err = launch_exact_glynn<32, 7>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<32, 7>();
         return true;
-    case 283:
-        if (args) *err = launch_exact_glynn<35, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<35, 3>();
+    case 549:
+        if (args) *err = launch_exact_glynn<34, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<34, 5>();
         return true;
-    case 299:
-        if (args) *err = launch_exact_glynn<37, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<37, 3>();
+    case 579:
+        if (args) *err = launch_exact_glynn<36, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<36, 3>();
         return true;
-    case 315:
-        if (args) *err = launch_exact_glynn<39, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<39, 3>();
+    case 600:
+        if (args) *err = launch_exact_glynn<37, 8>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<37, 8>();
         return true;
-    case 331:
-        if (args) *err = launch_exact_glynn<41, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<41, 3>();
+    case 630:
+        if (args) *err = launch_exact_glynn<39, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<39, 6>();
         return true;
-    case 347:
-        if (args) *err = launch_exact_glynn<43, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<43, 3>();
+    case 660:
+        if (args) *err = launch_exact_glynn<41, 4>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<41, 4>();
         return true;
-    case 363:
-        if (args) *err = launch_exact_glynn<45, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<45, 3>();
+    case 682:
+        if (args) *err = launch_exact_glynn<42, 10>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<42, 10>();
         return true;
-    case 379:
-        if (args) *err = launch_exact_glynn<47, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<47, 3>();
+    case 711:
+        if (args) *err = launch_exact_glynn<44, 7>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<44, 7>();
         return true;
-    default: return false;
+    case 741:
+        if (args) *err = launch_exact_glynn<46, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<46, 5>();
+        return true;
+    case 771:
+        if (args) *err = launch_exact_glynn<48, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<48, 3>();
+        return true;
+    default:
+        return false;
     }
 }
 

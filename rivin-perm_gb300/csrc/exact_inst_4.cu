@@ -1,104 +1,102 @@
-// Instantiations of the exact Glynn kernel (part 4 of 8).
+// Instantiations of the exact Glynn kernel (part 4 of 12),
+// written by gen_exact_inst.py.
 #include "exact_glynn.cuh"
 
 namespace pg {
 
 bool exact_dispatch_4(int N, int G, const ExactArgs *args, int blocks,
                        cudaStream_t stream, cudaError_t *err, int *occ) {
-    switch (N * 8 + G) {
-    case 27:
+    switch (N * 16 + G) {
+    case 51:
         if (args) *err = launch_exact_glynn<3, 3>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<3, 3>();
         return true;
-    case 44:
-        if (args) *err = launch_exact_glynn<5, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<5, 4>();
+    case 100:
+        if (args) *err = launch_exact_glynn<6, 4>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<6, 4>();
         return true;
-    case 60:
-        if (args) *err = launch_exact_glynn<7, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<7, 4>();
-        return true;
-    case 76:
+    case 148:
         if (args) *err = launch_exact_glynn<9, 4>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<9, 4>();
         return true;
-    case 92:
-        if (args) *err = launch_exact_glynn<11, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<11, 4>();
+    case 196:
+        if (args) *err = launch_exact_glynn<12, 4>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<12, 4>();
         return true;
-    case 108:
-        if (args) *err = launch_exact_glynn<13, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<13, 4>();
-        return true;
-    case 124:
+    case 244:
         if (args) *err = launch_exact_glynn<15, 4>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<15, 4>();
         return true;
-    case 146:
-        if (args) *err = launch_exact_glynn<18, 2>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<18, 2>();
+    case 307:
+        if (args) *err = launch_exact_glynn<19, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<19, 3>();
         return true;
-    case 164:
-        if (args) *err = launch_exact_glynn<20, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<20, 4>();
-        return true;
-    case 187:
+    case 371:
         if (args) *err = launch_exact_glynn<23, 3>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<23, 3>();
         return true;
-    case 203:
-        if (args) *err = launch_exact_glynn<25, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<25, 3>();
+    case 404:
+        if (args) *err = launch_exact_glynn<25, 4>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<25, 4>();
         return true;
-    case 214:
-        if (args) *err = launch_exact_glynn<26, 6>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<26, 6>();
+    case 424:
+        if (args) *err = launch_exact_glynn<26, 8>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<26, 8>();
         return true;
-    case 228:
+    case 452:
         if (args) *err = launch_exact_glynn<28, 4>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<28, 4>();
         return true;
-    case 242:
-        if (args) *err = launch_exact_glynn<30, 2>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<30, 2>();
+    case 472:
+        if (args) *err = launch_exact_glynn<29, 8>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<29, 8>();
         return true;
-    case 253:
-        if (args) *err = launch_exact_glynn<31, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<31, 5>();
+    case 500:
+        if (args) *err = launch_exact_glynn<31, 4>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<31, 4>();
         return true;
-    case 268:
-        if (args) *err = launch_exact_glynn<33, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<33, 4>();
+    case 520:
+        if (args) *err = launch_exact_glynn<32, 8>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<32, 8>();
         return true;
-    case 284:
-        if (args) *err = launch_exact_glynn<35, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<35, 4>();
+    case 550:
+        if (args) *err = launch_exact_glynn<34, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<34, 6>();
         return true;
-    case 300:
-        if (args) *err = launch_exact_glynn<37, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<37, 4>();
+    case 580:
+        if (args) *err = launch_exact_glynn<36, 4>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<36, 4>();
         return true;
-    case 316:
-        if (args) *err = launch_exact_glynn<39, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<39, 4>();
+    case 602:
+        if (args) *err = launch_exact_glynn<37, 10>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<37, 10>();
         return true;
-    case 332:
-        if (args) *err = launch_exact_glynn<41, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<41, 4>();
+    case 631:
+        if (args) *err = launch_exact_glynn<39, 7>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<39, 7>();
         return true;
-    case 348:
-        if (args) *err = launch_exact_glynn<43, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<43, 4>();
+    case 661:
+        if (args) *err = launch_exact_glynn<41, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<41, 5>();
         return true;
-    case 364:
-        if (args) *err = launch_exact_glynn<45, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<45, 4>();
+    case 691:
+        if (args) *err = launch_exact_glynn<43, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<43, 3>();
         return true;
-    case 380:
-        if (args) *err = launch_exact_glynn<47, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<47, 4>();
+    case 712:
+        if (args) *err = launch_exact_glynn<44, 8>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<44, 8>();
         return true;
-    default: return false;
+    case 742:
+        if (args) *err = launch_exact_glynn<46, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<46, 6>();
+        return true;
+    case 772:
+        if (args) *err = launch_exact_glynn<48, 4>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<48, 4>();
+        return true;
+    default:
+        return false;
     }
 }
 

@@ -1,104 +1,102 @@
-// Instantiations of the exact Glynn kernel (part 5 of 8).
+// Instantiations of the exact Glynn kernel (part 5 of 12),
+// written by gen_exact_inst.py.
 #include "exact_glynn.cuh"
 
 namespace pg {
 
 bool exact_dispatch_5(int N, int G, const ExactArgs *args, int blocks,
                        cudaStream_t stream, cudaError_t *err, int *occ) {
-    switch (N * 8 + G) {
-    case 33:
+    switch (N * 16 + G) {
+    case 65:
         if (args) *err = launch_exact_glynn<4, 1>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<4, 1>();
         return true;
-    case 49:
-        if (args) *err = launch_exact_glynn<6, 1>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<6, 1>();
+    case 113:
+        if (args) *err = launch_exact_glynn<7, 1>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<7, 1>();
         return true;
-    case 65:
-        if (args) *err = launch_exact_glynn<8, 1>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<8, 1>();
-        return true;
-    case 81:
+    case 161:
         if (args) *err = launch_exact_glynn<10, 1>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<10, 1>();
         return true;
-    case 97:
-        if (args) *err = launch_exact_glynn<12, 1>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<12, 1>();
+    case 209:
+        if (args) *err = launch_exact_glynn<13, 1>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<13, 1>();
         return true;
-    case 113:
-        if (args) *err = launch_exact_glynn<14, 1>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<14, 1>();
-        return true;
-    case 129:
+    case 257:
         if (args) *err = launch_exact_glynn<16, 1>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<16, 1>();
         return true;
-    case 147:
-        if (args) *err = launch_exact_glynn<18, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<18, 3>();
+    case 308:
+        if (args) *err = launch_exact_glynn<19, 4>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<19, 4>();
         return true;
-    case 170:
-        if (args) *err = launch_exact_glynn<21, 2>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<21, 2>();
-        return true;
-    case 188:
+    case 372:
         if (args) *err = launch_exact_glynn<23, 4>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<23, 4>();
         return true;
-    case 204:
-        if (args) *err = launch_exact_glynn<25, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<25, 4>();
+    case 405:
+        if (args) *err = launch_exact_glynn<25, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<25, 5>();
         return true;
-    case 218:
-        if (args) *err = launch_exact_glynn<27, 2>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<27, 2>();
+    case 426:
+        if (args) *err = launch_exact_glynn<26, 10>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<26, 10>();
         return true;
-    case 229:
+    case 453:
         if (args) *err = launch_exact_glynn<28, 5>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<28, 5>();
         return true;
-    case 243:
-        if (args) *err = launch_exact_glynn<30, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<30, 3>();
+    case 474:
+        if (args) *err = launch_exact_glynn<29, 10>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<29, 10>();
         return true;
-    case 254:
-        if (args) *err = launch_exact_glynn<31, 6>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<31, 6>();
+    case 501:
+        if (args) *err = launch_exact_glynn<31, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<31, 5>();
         return true;
-    case 269:
-        if (args) *err = launch_exact_glynn<33, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<33, 5>();
+    case 522:
+        if (args) *err = launch_exact_glynn<32, 10>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<32, 10>();
         return true;
-    case 285:
-        if (args) *err = launch_exact_glynn<35, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<35, 5>();
+    case 551:
+        if (args) *err = launch_exact_glynn<34, 7>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<34, 7>();
         return true;
-    case 301:
-        if (args) *err = launch_exact_glynn<37, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<37, 5>();
+    case 581:
+        if (args) *err = launch_exact_glynn<36, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<36, 5>();
         return true;
-    case 317:
-        if (args) *err = launch_exact_glynn<39, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<39, 5>();
+    case 611:
+        if (args) *err = launch_exact_glynn<38, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<38, 3>();
         return true;
-    case 333:
-        if (args) *err = launch_exact_glynn<41, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<41, 5>();
+    case 632:
+        if (args) *err = launch_exact_glynn<39, 8>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<39, 8>();
         return true;
-    case 349:
-        if (args) *err = launch_exact_glynn<43, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<43, 5>();
+    case 662:
+        if (args) *err = launch_exact_glynn<41, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<41, 6>();
         return true;
-    case 365:
-        if (args) *err = launch_exact_glynn<45, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<45, 5>();
+    case 692:
+        if (args) *err = launch_exact_glynn<43, 4>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<43, 4>();
         return true;
-    case 381:
-        if (args) *err = launch_exact_glynn<47, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<47, 5>();
+    case 714:
+        if (args) *err = launch_exact_glynn<44, 10>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<44, 10>();
         return true;
-    default: return false;
+    case 743:
+        if (args) *err = launch_exact_glynn<46, 7>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<46, 7>();
+        return true;
+    case 773:
+        if (args) *err = launch_exact_glynn<48, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<48, 5>();
+        return true;
+    default:
+        return false;
     }
 }
 

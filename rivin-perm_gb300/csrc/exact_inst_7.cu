@@ -1,104 +1,102 @@
-// Instantiations of the exact Glynn kernel (part 7 of 8).
+// Instantiations of the exact Glynn kernel (part 7 of 12),
+// written by gen_exact_inst.py.
 #include "exact_glynn.cuh"
 
 namespace pg {
 
 bool exact_dispatch_7(int N, int G, const ExactArgs *args, int blocks,
                        cudaStream_t stream, cudaError_t *err, int *occ) {
-    switch (N * 8 + G) {
-    case 35:
+    switch (N * 16 + G) {
+    case 67:
         if (args) *err = launch_exact_glynn<4, 3>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<4, 3>();
         return true;
-    case 51:
-        if (args) *err = launch_exact_glynn<6, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<6, 3>();
+    case 115:
+        if (args) *err = launch_exact_glynn<7, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<7, 3>();
         return true;
-    case 67:
-        if (args) *err = launch_exact_glynn<8, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<8, 3>();
-        return true;
-    case 83:
+    case 163:
         if (args) *err = launch_exact_glynn<10, 3>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<10, 3>();
         return true;
-    case 99:
-        if (args) *err = launch_exact_glynn<12, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<12, 3>();
+    case 211:
+        if (args) *err = launch_exact_glynn<13, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<13, 3>();
         return true;
-    case 115:
-        if (args) *err = launch_exact_glynn<14, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<14, 3>();
-        return true;
-    case 131:
+    case 259:
         if (args) *err = launch_exact_glynn<16, 3>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<16, 3>();
         return true;
-    case 154:
-        if (args) *err = launch_exact_glynn<19, 2>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<19, 2>();
+    case 323:
+        if (args) *err = launch_exact_glynn<20, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<20, 3>();
         return true;
-    case 172:
-        if (args) *err = launch_exact_glynn<21, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<21, 4>();
-        return true;
-    case 195:
+    case 387:
         if (args) *err = launch_exact_glynn<24, 3>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<24, 3>();
         return true;
-    case 206:
-        if (args) *err = launch_exact_glynn<25, 6>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<25, 6>();
+    case 407:
+        if (args) *err = launch_exact_glynn<25, 7>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<25, 7>();
         return true;
-    case 220:
-        if (args) *err = launch_exact_glynn<27, 4>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<27, 4>();
+    case 435:
+        if (args) *err = launch_exact_glynn<27, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<27, 3>();
         return true;
-    case 234:
-        if (args) *err = launch_exact_glynn<29, 2>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<29, 2>();
+    case 455:
+        if (args) *err = launch_exact_glynn<28, 7>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<28, 7>();
         return true;
-    case 245:
-        if (args) *err = launch_exact_glynn<30, 5>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<30, 5>();
+    case 483:
+        if (args) *err = launch_exact_glynn<30, 3>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<30, 3>();
         return true;
-    case 259:
-        if (args) *err = launch_exact_glynn<32, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<32, 3>();
+    case 503:
+        if (args) *err = launch_exact_glynn<31, 7>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<31, 7>();
         return true;
-    case 275:
-        if (args) *err = launch_exact_glynn<34, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<34, 3>();
+    case 532:
+        if (args) *err = launch_exact_glynn<33, 4>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<33, 4>();
         return true;
-    case 291:
-        if (args) *err = launch_exact_glynn<36, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<36, 3>();
+    case 554:
+        if (args) *err = launch_exact_glynn<34, 10>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<34, 10>();
         return true;
-    case 307:
-        if (args) *err = launch_exact_glynn<38, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<38, 3>();
+    case 583:
+        if (args) *err = launch_exact_glynn<36, 7>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<36, 7>();
         return true;
-    case 323:
+    case 613:
+        if (args) *err = launch_exact_glynn<38, 5>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<38, 5>();
+        return true;
+    case 643:
         if (args) *err = launch_exact_glynn<40, 3>(*args, blocks, stream);
         if (occ) *occ = occupancy_exact_glynn<40, 3>();
         return true;
-    case 339:
-        if (args) *err = launch_exact_glynn<42, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<42, 3>();
+    case 664:
+        if (args) *err = launch_exact_glynn<41, 8>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<41, 8>();
         return true;
-    case 355:
-        if (args) *err = launch_exact_glynn<44, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<44, 3>();
+    case 694:
+        if (args) *err = launch_exact_glynn<43, 6>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<43, 6>();
         return true;
-    case 371:
-        if (args) *err = launch_exact_glynn<46, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<46, 3>();
+    case 724:
+        if (args) *err = launch_exact_glynn<45, 4>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<45, 4>();
         return true;
-    case 387:
-        if (args) *err = launch_exact_glynn<48, 3>(*args, blocks, stream);
-        if (occ) *occ = occupancy_exact_glynn<48, 3>();
+    case 746:
+        if (args) *err = launch_exact_glynn<46, 10>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<46, 10>();
         return true;
-    default: return false;
+    case 775:
+        if (args) *err = launch_exact_glynn<48, 7>(*args, blocks, stream);
+        if (occ) *occ = occupancy_exact_glynn<48, 7>();
+        return true;
+    default:
+        return false;
     }
 }
 

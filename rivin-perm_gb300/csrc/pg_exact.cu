@@ -18,7 +18,7 @@ static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 static bool try_grouping(const uint64_t *B, int n, int G, bool small_last, int *order) {
     const int NG = (n + G - 1) / G;
     const int last_cap = n - (NG - 1) * G;
-    int idx[48], cnt[48] = {0}, mem[48][8];
+    int idx[48], cnt[48] = {0}, mem[48][EXACT_MAX_G];
     double lp[48] = {0};
     for (int i = 0; i < n; i++) idx[i] = i;
     for (int i = 1; i < n; i++)                    // stable, descending B
@@ -52,11 +52,12 @@ static bool try_grouping(const uint64_t *B, int n, int G, bool small_last, int *
 }
 
 bool exact_group_rows(const uint64_t *B, int n, int G, int *order) {
-    if (n < 1 || n > 48 || G < 1 || G > 8) return false;
+    if (n < 1 || n > 48 || G < 1 || G > EXACT_MAX_G) return false;
     return try_grouping(B, n, G, false, order) || try_grouping(B, n, G, true, order);
 }
 
-// Picks the largest compiled group size that admits a grouping.
+// Picks the largest compiled group size that admits a grouping (fewest
+// product words).
 static int choose_group(const int64_t *A, int n, std::vector<int> *order) {
     if (n < 2 || n > 48) return 0;
     std::vector<uint64_t> B(n);
@@ -70,7 +71,7 @@ static int choose_group(const int64_t *A, int n, std::vector<int> *order) {
         B[i] = (uint64_t)s;
     }
     order->resize(n);
-    for (int G = 6; G >= 1; G--) {
+    for (int G = EXACT_MAX_G; G >= 1; G--) {
         if (!exact_compiled(n, G)) continue;
         if (exact_group_rows(B.data(), n, G, order->data())) return G;
     }

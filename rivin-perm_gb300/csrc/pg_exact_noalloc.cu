@@ -85,7 +85,7 @@ extern "C" int pg_exact_permanent_noalloc(const int64_t *A, int n, uint32_t *out
     if (32.0 * limbs < bits + 2)
         return fail(PG_ERANGE, "output limb count too small for the permanent bound");
     int order[48], G = 0;
-    for (int g = 6; g >= 1 && !G; g--) {
+    for (int g = EXACT_MAX_G; g >= 1 && !G; g--) {
         if (!exact_compiled(n, g)) continue;
         if (!exact_group_rows(B, n, g, order)) continue;
         G = g;
