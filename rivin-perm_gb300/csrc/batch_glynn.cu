@@ -41,6 +41,7 @@ struct BatchArgs {
     const int32_t *tables;        // concatenated [tab | init] per matrix
     const uint64_t *table_off;    // int32 offset of each matrix's table
     const uint8_t *orders;        // n per matrix
+    const uint8_t *groups;        // row-group size G per matrix
     const uint8_t *log_len;       // chunk log length per matrix
     const uint64_t *chunks;       // chunks per matrix
     const BatchTask *tasks;
@@ -51,10 +52,18 @@ struct BatchArgs {
     volatile const int *abort_flag;
 };
 
-template <int N>
+// Group sizes compiled into the batch kernel: 4 (N < 4: N) for every order
+// and 5 for orders 20..32, where the time of a batch goes; the host takes
+// the largest whose groups fit (small entries: fewer product words per term).
+__host__ __device__ constexpr bool batch_compiled(int N, int G) {
+    return N < 2 || N > BATCH_MAX_N ? false
+           : N < 4 ? G == N
+           : G == 4 || (G == 5 && N >= 20);
+}
+
+template <int N, int G>
 __device__ __forceinline__ void batch_task(const int32_t *wtab, const BatchArgs &a,
                                            const BatchTask &t, int lane) {
-    constexpr int G = N >= 4 ? 4 : N;
     using S = ExactShape<N, G>;
     constexpr int NP = S::NP, NL = S::NL;
     // the warp slice stores rows with stride BATCH_NP; exact_walk indexes
@@ -106,16 +115,23 @@ __global__ void __launch_bounds__(256, 2) batch_glynn_kernel(BatchArgs a) {
             __syncwarp();
             cur = t.m;
         }
-        switch (n) {
-#define PG_BATCH_CASE(NN) case NN: batch_task<NN>(wtab, a, t, lane); break;
-            PG_BATCH_CASE(2) PG_BATCH_CASE(3) PG_BATCH_CASE(4) PG_BATCH_CASE(5)
-            PG_BATCH_CASE(6) PG_BATCH_CASE(7) PG_BATCH_CASE(8) PG_BATCH_CASE(9)
-            PG_BATCH_CASE(10) PG_BATCH_CASE(11) PG_BATCH_CASE(12) PG_BATCH_CASE(13)
-            PG_BATCH_CASE(14) PG_BATCH_CASE(15) PG_BATCH_CASE(16) PG_BATCH_CASE(17)
-            PG_BATCH_CASE(18) PG_BATCH_CASE(19) PG_BATCH_CASE(20) PG_BATCH_CASE(21)
-            PG_BATCH_CASE(22) PG_BATCH_CASE(23) PG_BATCH_CASE(24) PG_BATCH_CASE(25)
-            PG_BATCH_CASE(26) PG_BATCH_CASE(27) PG_BATCH_CASE(28) PG_BATCH_CASE(29)
-            PG_BATCH_CASE(30) PG_BATCH_CASE(31) PG_BATCH_CASE(32)
+        switch (n * 8 + a.groups[t.m]) {
+#define PG_BATCH_CASE(NN, GG) case NN * 8 + GG: batch_task<NN, GG>(wtab, a, t, lane); break;
+            PG_BATCH_CASE(2, 2) PG_BATCH_CASE(3, 3)
+#define PG_BATCH_G4(NN) PG_BATCH_CASE(NN, 4)
+#define PG_BATCH_G5(NN) PG_BATCH_CASE(NN, 5)
+            PG_BATCH_G4(4) PG_BATCH_G4(5) PG_BATCH_G4(6) PG_BATCH_G4(7) PG_BATCH_G4(8)
+            PG_BATCH_G4(9) PG_BATCH_G4(10) PG_BATCH_G4(11) PG_BATCH_G4(12) PG_BATCH_G4(13)
+            PG_BATCH_G4(14) PG_BATCH_G4(15) PG_BATCH_G4(16) PG_BATCH_G4(17) PG_BATCH_G4(18)
+            PG_BATCH_G4(19) PG_BATCH_G4(20) PG_BATCH_G4(21) PG_BATCH_G4(22) PG_BATCH_G4(23)
+            PG_BATCH_G4(24) PG_BATCH_G4(25) PG_BATCH_G4(26) PG_BATCH_G4(27) PG_BATCH_G4(28)
+            PG_BATCH_G4(29) PG_BATCH_G4(30) PG_BATCH_G4(31) PG_BATCH_G4(32)
+            PG_BATCH_G5(20)
+            PG_BATCH_G5(21) PG_BATCH_G5(22) PG_BATCH_G5(23) PG_BATCH_G5(24) PG_BATCH_G5(25)
+            PG_BATCH_G5(26) PG_BATCH_G5(27) PG_BATCH_G5(28) PG_BATCH_G5(29) PG_BATCH_G5(30)
+            PG_BATCH_G5(31) PG_BATCH_G5(32)
+#undef PG_BATCH_G4
+#undef PG_BATCH_G5
 #undef PG_BATCH_CASE
         default: break;
         }
@@ -138,9 +154,9 @@ static void add_i64_at(std::vector<uint32_t> &w, int pos, long long v) {
     }
 }
 
-// Row order for groups of 4 (exact_group_rows), or false.
-static bool batch_group(const int64_t *A, int n, std::vector<int> *order) {
-    const int G = n >= 4 ? 4 : n;
+// Row order for the largest compiled group size whose groups fit
+// (exact_group_rows); returns that size, or 0.
+static int batch_group(const int64_t *A, int n, std::vector<int> *order) {
     std::vector<uint64_t> B(n);
     for (int i = 0; i < n; i++) {
         unsigned __int128 s = 0;
@@ -148,16 +164,19 @@ static bool batch_group(const int64_t *A, int n, std::vector<int> *order) {
             const int64_t v = A[(size_t)i * n + j];
             s += v < 0 ? (unsigned __int128)(-(__int128)v) : (unsigned __int128)v;
         }
-        if (s >= ((unsigned __int128)1 << 30)) return false;
+        if (s >= ((unsigned __int128)1 << 30)) return 0;
         B[i] = (uint64_t)s;
     }
     order->resize(n);
-    return exact_group_rows(B.data(), n, G, order->data());
+    for (int G = 5; G >= 2; G--)
+        if (batch_compiled(n, G) && exact_group_rows(B.data(), n, G, order->data())) return G;
+    return 0;
 }
 
 struct BatchPlan {
     int count = 0;
     std::vector<int> orders;
+    std::vector<uint8_t> groups;           // row-group size of each kernel matrix
     std::vector<uint8_t> in_kernel;        // 1 if the batch kernel evaluates it
     std::vector<std::vector<int64_t>> external;  // matrices for the single engine
     std::vector<int> ext_index;
@@ -206,6 +225,7 @@ int pg_batch_plan_create(const int64_t *A, const int64_t *offsets, const int32_t
     P.count = count;
     P.orders.assign(orders, orders + count);
     P.in_kernel.assign(count, 0);
+    P.groups.assign(count, 0);
     P.ext_index.assign(count, -1);
     P.bound_bits.assign(count, 0.0);
 
@@ -226,12 +246,14 @@ int pg_batch_plan_create(const int64_t *A, const int64_t *offsets, const int32_t
         }
         P.bound_bits[m] = bits;
         std::vector<int> order;
-        if (n < 2 || n > BATCH_MAX_N || !batch_group(a, n, &order)) {
+        const int G = n < 2 || n > BATCH_MAX_N ? 0 : batch_group(a, n, &order);
+        if (!G) {
             P.ext_index[m] = (int)P.external.size();
             P.external.emplace_back(a, a + (size_t)n * n);
             continue;
         }
         P.in_kernel[m] = 1;
+        P.groups[m] = (uint8_t)G;
         const int NP = (n + 3) & ~3;
         toff[m] = tables.size();
         const size_t base = tables.size();
@@ -278,7 +300,8 @@ int pg_batch_plan_create(const int64_t *A, const int64_t *offsets, const int32_t
     const size_t off_tables = 0;
     const size_t off_toff = align_up(off_tables + tables.size() * 4, 256);
     const size_t off_ord = align_up(off_toff + (size_t)count * 8, 256);
-    const size_t off_ll = align_up(off_ord + (size_t)count, 256);
+    const size_t off_grp = align_up(off_ord + (size_t)count, 256);
+    const size_t off_ll = align_up(off_grp + (size_t)count, 256);
     const size_t off_nch = align_up(off_ll + (size_t)count, 256);
     const size_t off_tasks = align_up(off_nch + (size_t)count * 8, 256);
     P.off_acc = align_up(off_tasks + sorted.size() * sizeof(BatchTask), 256);
@@ -298,6 +321,7 @@ int pg_batch_plan_create(const int64_t *A, const int64_t *offsets, const int32_t
     if (!tables.empty()) std::memcpy(P.host + off_tables, tables.data(), tables.size() * 4);
     std::memcpy(P.host + off_toff, toff.data(), (size_t)count * 8);
     std::memcpy(P.host + off_ord, ord8.data(), (size_t)count);
+    if (count) std::memcpy(P.host + off_grp, P.groups.data(), (size_t)count);
     std::memcpy(P.host + off_ll, loglen.data(), (size_t)count);
     std::memcpy(P.host + off_nch, nchunks.data(), (size_t)count * 8);
     if (!sorted.empty())
@@ -314,6 +338,7 @@ int pg_batch_plan_create(const int64_t *A, const int64_t *offsets, const int32_t
     a.tables = (const int32_t *)(P.dev + off_tables);
     a.table_off = (const uint64_t *)(P.dev + off_toff);
     a.orders = (const uint8_t *)(P.dev + off_ord);
+    a.groups = (const uint8_t *)(P.dev + off_grp);
     a.log_len = (const uint8_t *)(P.dev + off_ll);
     a.chunks = (const uint64_t *)(P.dev + off_nch);
     a.tasks = (const BatchTask *)(P.dev + off_tasks);
@@ -386,7 +411,7 @@ int pg_batch_plan_result(pg_batch_plan *plan, void *stream, uint32_t *out, int l
         }
         const int W = BATCH_WORDS + 3;
         std::vector<uint32_t> S(W, 0);
-        const int G = n >= 4 ? 4 : n;
+        const int G = P.groups[m];
         const int NL = (n + G - 1) / G + 1;
         for (int l = 0; l < NL; l++) add_i64_at(S, l, acc[(size_t)m * BATCH_WORDS + l]);
         const int sh = n - 1;
