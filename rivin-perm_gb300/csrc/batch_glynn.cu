@@ -8,7 +8,7 @@
 // decreasing work (largest orders first) so the tail is made of small
 // tasks.  Each task's per-word sums are warp-reduced and added to the
 // matrix's 64-bit words with one atomic per word.  Orders 2..32 are compiled
-// (row groups of 4, as in the single-matrix engine); matrices outside that
+// (row groups of 4, and of 5 from order 20: batch_compiled); matrices outside that
 // range or whose groups do not fit are evaluated by the single-matrix exact
 // engine when the results are collected.
 //
