@@ -36,3 +36,21 @@ def test_library_exports_every_declared_symbol():
 def test_ctypes_signatures_cover_header():
     from permgpu import _lib
     assert set(declared_symbols()) <= set(_lib.SIGNATURES)
+
+
+def test_exact_instantiations_match_their_generator(tmp_path):
+    # exact_inst_*.cu and exact_dispatch.cu are written by gen_exact_inst.py;
+    # regenerating into a scratch copy must reproduce them byte for byte
+    import importlib.util
+    import shutil
+    from pathlib import Path
+    csrc = Path(__file__).resolve().parents[1] / "rivin-perm_gb300" / "csrc"
+    shutil.copy(csrc / "gen_exact_inst.py", tmp_path / "gen_exact_inst.py")
+    spec = importlib.util.spec_from_file_location("gen_exact_inst", tmp_path / "gen_exact_inst.py")
+    gen = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(gen)
+    gen.main()
+    made = sorted(p.name for p in tmp_path.glob("exact_*.cu"))
+    assert made == sorted(p.name for p in csrc.glob("exact_*.cu"))
+    for name in made:
+        assert (tmp_path / name).read_text() == (csrc / name).read_text(), name
