@@ -289,9 +289,11 @@ def run_gpu(args, world, rank, local):
     e2e_step = max_over_ranks(world, statistics.mean(e2e_s))
     value = world * states / (step_ms * 1e-3)
     e2e_value = world * states / e2e_step
-    # roofline: IMAD-pipe work counted from the kernel source, in mad.lo.u32
-    # equivalents.  With NG product words a term is n - NG IMUL (row-group
-    # products), (NG-2)(NG-1)/2 mul.wide.u32 (the running product) and
+    # roofline: the algorithm's multiplies counted from the kernel source, in
+    # mad.lo.u32 equivalents.  With NG product words a term is n - NG 32-bit
+    # row-group multiplies (for small-entry matrices two of every three run
+    # as exact FP32 multiplies on the FP32 pipe; they are counted all the
+    # same), (NG-2)(NG-1)/2 mul.wide.u32 (the running product) and
     # max(NG-1, 1) mad.wide.u32 into the 64-bit columns.  Every 32x32->64
     # product is weighted by the measured mul.wide.u32 : mad.lo.u32 rate
     # ratio (about 2).  The mad.wide probe (64-bit addend) runs slower still

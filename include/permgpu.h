@@ -186,8 +186,10 @@ int pg_exact_plan_create(const int64_t *A, int n, pg_exact_plan **plan);
 int pg_exact_plan_launch(pg_exact_plan *plan, void *stream);
 int pg_exact_plan_result(pg_exact_plan *plan, void *stream, uint32_t *out,
                          int limbs);
-/* group size, product words, Gray states, and per-state 32-bit IMUL and
- * mad.wide.u32 counts of the launch (the roofline's work unit). */
+/* group size, product words, Gray states, and per-state counts of 32-bit
+ * row-group multiplies and 32x32->64 word products of the launch (the
+ * roofline's work unit; the float-row form runs two of every three group
+ * multiplies as exact FP32 multiplies). */
 int pg_exact_plan_info(const pg_exact_plan *plan, int *group, int *words,
                        uint64_t *states, uint64_t *imul_per_state,
                        uint64_t *imad_wide_per_state);
