@@ -53,6 +53,27 @@ def test_group_sizes_agree(lib, G):
     assert lib.exact_permanent(a, lib.exact_limbs(a)) == oracle.exact_permanent(a.tolist())
 
 
+@pytest.mark.parametrize("n", [24, 28, 32])
+def test_float_row_form_and_its_fallback(lib, n):
+    # entries in [-8, 8] take the float-row form at these orders (three rows
+    # of every group of 4 as exact FP32 sums); half the rows with large
+    # entries put two large rows in a group (three-row bound product above
+    # 2^22, or groups of 3: integer form), and
+    # rows of mixed bounds make the host put the largest row of each group
+    # last.  Every result must equal the residue engine's at several primes.
+    rng = np.random.default_rng(700 + n)
+    primes = [2_147_483_647, 2_147_483_629, 1_000_000_007, 4_294_967_291]
+    base = rng.integers(-8, 9, (n, n), dtype=np.int64)
+    mixed = base.copy()
+    mixed[::3] = rng.integers(-2, 3, (len(mixed[::3]), n))
+    wide = base.copy()
+    wide[::2] = rng.integers(-40, 41, (n // 2, n))
+    for a in (base, mixed, wide):
+        assert lib.exact_supported(a)
+        v = lib.exact_permanent(a, lib.exact_limbs(a))
+        assert lib.residues(a, primes) == [v % p for p in primes]
+
+
 def test_exact_extremes(lib):
     # all-ones, negative identity, zero row, large entries near the limit
     for n in (5, 12, 20):
