@@ -546,11 +546,14 @@ def run_gpu_poly(args, world, rank, local):
     bounds = poly._bounds(tuple((1,) * n for _ in range(n)), am)
     primes = poly._gpu_primes(max(bounds))
     states = len(primes) * (1 << (n - 1))
-    # IMAD-pipe work per state in mad.lo.u32 slots: factor r = 1..n-1 costs
-    # two plain reductions (mul.wide, mul.lo, mad.wide) and r fused
-    # two-product reductions (mul.wide, mad.wide, mul.lo, mad.wide); every
-    # 32x32->64 product is weighted by the measured mul.wide : mad.lo ratio
-    imad_per_state = 2 * (n - 1) * (n + 3)
+    # C = J has equal rows, so the uniform kernel runs: per state the
+    # elementary-symmetric recurrence (factor r = 1..n-1: r Montgomery
+    # products), n - 1 powers of the common row sum and n weighted
+    # coefficients, n(n-1)/2 + 2n - 1 Montgomery products of mul.wide,
+    # mul.lo and mad.wide each; every 32x32->64 product is weighted by the
+    # measured mul.wide : mad.lo ratio
+    redc_per_state = n * (n - 1) // 2 + 2 * n - 1
+    imad_per_state = 3 * redc_per_state
     for _ in range(args.warmup):
         got = permgpu.rook_polynomial(a.tolist())
         _lib.affine_residues(ones, a, primes)
@@ -559,7 +562,7 @@ def run_gpu_poly(args, world, rank, local):
     peak_lo = _lib.probe_int_throughput(0)
     peak = peak_lo / 1e12                         # mad.lo.u32 ops/s -> Tops/s
     w = peak_lo / _lib.probe_int_throughput(4)    # mul.wide.u32 weight
-    slots_per_state = 2 * (n - 1) * (2 * w + 1) + (3 * w + 1) * (n - 1) * n / 2
+    slots_per_state = redc_per_state * (2 * w + 1)
     clocks = ClockSampler(local).start()
     barrier(world)
     ts, te = [], []

@@ -21,25 +21,17 @@
 // one 64-bit word per coefficient into global memory.
 #include "pg_internal.h"
 #include "glynn_m32.cuh"
+#include "poly_common.cuh"
+
+// 1: matrices C with equal rows (rook polynomials) take the uniform kernel.
+#ifndef PG_POLY_UNIFORM
+#define PG_POLY_UNIFORM 1
+#endif
 
 #include <cstring>
 #include <vector>
 
 namespace pg {
-
-constexpr int POLY_MAX_N = 32;
-
-struct PolyArgs {
-    const uint32_t *tabs;     // [k][N-1][2 dir][2 (C, L)][NP]: (d - p) mod 2^32
-    const uint32_t *init;     // [k][2][NP]: row sums of C and L, all-plus state
-    const uint32_t *moduli;   // [k]
-    const uint32_t *pinvs;    // [k]  -p^-1 mod 2^32
-    unsigned long long *acc;  // [k][N+1] (zeroed)
-    int *status;
-    volatile const int *abort_flag;
-    uint64_t chunks;          // chunks per modulus
-    int log_len;
-};
 
 // (a*c + b*l) * 2^-32 mod p for a, b < 2p and c, l < p < 2^30: < 2p.
 __device__ __forceinline__ uint32_t poly_redc2(uint32_t a, uint32_t c, uint32_t b, uint32_t l,
@@ -48,14 +40,6 @@ __device__ __forceinline__ uint32_t poly_redc2(uint32_t a, uint32_t c, uint32_t 
     const uint32_t m = (uint32_t)t * pinv;
     return (uint32_t)(((uint64_t)m * p + t) >> 32);
 }
-
-// From order 20 on the n+1 coefficient accumulators move from registers to
-// shared memory (one word per coefficient and thread, thread-minor so a warp
-// touches 32 consecutive banks) and blocks shrink to 128 threads: the row
-// sums and the coefficient vector alone fill most of the register file, and
-// fewer registers per thread let three or more blocks share an SM.
-__host__ __device__ constexpr bool poly_acc_in_smem(int N) { return N >= 20; }
-__host__ __device__ constexpr int poly_block(int N) { return poly_acc_in_smem(N) ? 128 : 256; }
 
 template <int N>
 __global__ void __launch_bounds__(poly_block(N)) affine_m32_kernel(PolyArgs a) {
@@ -227,10 +211,101 @@ static cudaError_t launch_affine(int n, const PolyArgs &args, int k, int sm_coun
 
 static size_t poly_align(size_t v) { return (v + 255) / 256 * 256; }
 
+// True when every row of C equals the first (the rook case C = J): the
+// uniform kernel of pg_poly_uniform.cu then applies.
+static bool rows_equal(const int64_t *C, int n) {
+    for (int i = 1; i < n; i++)
+        for (int j = 0; j < n; j++)
+            if (C[(size_t)i * n + j] != C[j]) return false;
+    return true;
+}
+
+// The uniform kernel's launch: tables of L (Montgomery residues) plus the
+// common row sum of C, one R removed at the end.
+static int uniform_residues_impl(const int64_t *C, const int64_t *L, int n,
+                                 const uint64_t *moduli, int k, uint64_t *out) {
+    DeviceInfo dev;
+    int st = device_info(&dev);
+    if (st != PG_OK) return st;
+    volatile int *abort_dev;
+    st = abort_flag_device(&abort_dev);
+    if (st != PG_OK) return st;
+    const int NPU = poly_uniform_stride(n), NCOL = n - 1;
+    const size_t tab_words = (size_t)NCOL * 2 * NPU;
+    const size_t off_init = poly_align((size_t)k * tab_words * 4);
+    const size_t off_mod = poly_align(off_init + (size_t)k * NPU * 4);
+    const size_t off_pinv = poly_align(off_mod + (size_t)k * 4);
+    const size_t off_acc = poly_align(off_pinv + (size_t)k * 4);
+    const size_t off_status = poly_align(off_acc + (size_t)k * (n + 1) * 8);
+    const size_t total = poly_align(off_status + 16);
+    Workspace *ws;
+    st = workspace(&ws, total, total);
+    if (st != PG_OK) return st;
+    char *h = (char *)ws->host;
+    char *d = (char *)ws->dev;
+    std::memset(h, 0, total);
+    for (int t = 0; t < k; t++) {
+        const uint64_t p = moduli[t];
+        const uint64_t R = (1ull << 32) % p;
+        const auto mont = [&](uint64_t x) { return (uint32_t)mulmod_u64(x % p, R, p); };
+        uint32_t *tt = (uint32_t *)h + (size_t)t * tab_words;
+        uint32_t *init = (uint32_t *)(h + off_init) + (size_t)t * NPU;
+        // entry n of a row: the common row sum of C (row 0)
+        for (int i = 0; i <= n; i++) {
+            const int64_t *row = i < n ? L + (size_t)i * n : C;
+            uint64_t sum = 0;
+            for (int j = 0; j < n; j++) {
+                const uint64_t v = normmod_i64(row[j], p);
+                sum = (sum + v) % p;
+                if (j < NCOL) {
+                    const uint32_t v2 = mont(2 * v % p);
+                    // direction 0 (column back to +): add 2a; 1 (to -): subtract 2a
+                    tt[(2 * j + 0) * NPU + i] = v2 - (uint32_t)p;
+                    tt[(2 * j + 1) * NPU + i] = 0u - v2;
+                }
+            }
+            init[i] = mont(sum);
+        }
+        ((uint32_t *)(h + off_mod))[t] = (uint32_t)p;
+        ((uint32_t *)(h + off_pinv))[t] = neg_inv32((uint32_t)p);
+    }
+    const ChunkPlan pl = plan_chunks(n - 1, n - 1 < 6 ? n - 1 : 6, 1ull << 20);
+    PolyArgs a;
+    a.tabs = (const uint32_t *)d;
+    a.init = (const uint32_t *)(d + off_init);
+    a.moduli = (const uint32_t *)(d + off_mod);
+    a.pinvs = (const uint32_t *)(d + off_pinv);
+    a.acc = (unsigned long long *)(d + off_acc);
+    a.status = (int *)(d + off_status);
+    a.abort_flag = abort_dev;
+    a.chunks = pl.chunks;
+    a.log_len = pl.log_len;
+    PG_CUDA(cudaMemcpyAsync(d, h, off_acc, cudaMemcpyHostToDevice, ws->stream));
+    PG_CUDA(cudaMemsetAsync(d + off_acc, 0, total - off_acc, ws->stream));
+    PG_CUDA(launch_poly_uniform(n, a, k, dev.sm_count, ws->stream));
+    PG_CUDA(cudaMemcpyAsync(h + off_acc, d + off_acc, total - off_acc, cudaMemcpyDeviceToHost,
+                            ws->stream));
+    PG_CUDA(cudaStreamSynchronize(ws->stream));
+    if (*(int *)(h + off_status)) return fail(PG_EABORT, "launch aborted by pg_abort()");
+    const unsigned long long *acc = (const unsigned long long *)(h + off_acc);
+    for (int t = 0; t < k; t++) {
+        const uint64_t p = moduli[t];
+        // remove R = 2^32 (the values are Montgomery residues) and scale by
+        // 2^(1-n): multiply by 2^-(n+31), 2^-1 = (p+1)/2 for odd p
+        const uint64_t fix = powmod_u64((p >> 1) + 1, (uint64_t)(n + 31), p);
+        for (int dgr = 0; dgr <= n; dgr++)
+            out[(size_t)t * (n + 1) + dgr] = mulmod_u64(acc[(size_t)t * (n + 1) + dgr] % p, fix, p);
+    }
+    return PG_OK;
+}
+
 // out[t*(n+1) + d] = coefficient d of per(C + x L) mod moduli[t], 2 <= n <= 32,
 // odd moduli 3 <= m < 2^30, k <= 65535.
 static int affine_residues_impl(const int64_t *C, const int64_t *L, int n,
                                 const uint64_t *moduli, int k, uint64_t *out) {
+#if PG_POLY_UNIFORM
+    if (rows_equal(C, n)) return uniform_residues_impl(C, L, n, moduli, k, out);
+#endif
     DeviceInfo dev;
     int st = device_info(&dev);
     if (st != PG_OK) return st;

@@ -26,6 +26,26 @@ def test_residues_match_oracle(lib, n):
         assert row == oracle.affine_mod_p(c, l, m), (n, m)
 
 
+@pytest.mark.parametrize("n", [2, 3, 5, 8, 13, 19, 20, 22])
+def test_equal_row_kernel_matches_oracle(lib, n):
+    # C with equal rows (all ones, or one random row repeated) takes the
+    # uniform kernel: elementary symmetric sums of the L row sums weighted
+    # by powers of the common C row sum
+    rng = np.random.default_rng(950 + n)
+    l = rng.integers(-9, 10, (n, n))
+    for c in (np.ones((n, n), dtype=np.int64),
+              np.tile(rng.integers(-(1 << 40), 1 << 40, n), (n, 1))):
+        got = lib.affine_residues(c, l, MODULI)
+        for m, row in zip(MODULI, got):
+            assert row == oracle.affine_mod_p(c, l, m), (n, m)
+    # one differing entry sends the matrix back to the general kernel
+    c = np.ones((n, n), dtype=np.int64)
+    c[n - 1, 0] = 2
+    got = lib.affine_residues(c, l, MODULI)
+    for m, row in zip(MODULI, got):
+        assert row == oracle.affine_mod_p(c, l, m), (n, m)
+
+
 def test_exact_vectors_match_reference():
     import permgpu
     data = golden("poly.json")
