@@ -277,6 +277,16 @@ int pg_glynn_c64_dev(const double *Are, const double *Aim, int batch, int n,
                      void *stream);
 
 /*
+ * pg_glynn_c64_dev with host pointers: real and imaginary planes
+ * [batch][n][n] in, per_re/per_im[batch] and abs_sum[batch] (nullable) out;
+ * 0 <= n <= 32.  Device buffers for the call are allocated and freed
+ * inside.  Replaces permanent_parallel_complex (perm_parallel_cuda.cu:
+ * 416-498) for a whole batch.
+ */
+int pg_glynn_c64(const double *Are, const double *Aim, int batch, int n,
+                 double *per_re, double *per_im, double *abs_sum);
+
+/*
  * pg_exact_permanent for callers that cannot allocate memory (no
  * counterpart in the reference).  Code that runs during CUDA graph capture,
  * plug-ins whose host owns every device allocation, and services that must

@@ -598,3 +598,51 @@ extern "C" int pg_glynn_f64_fwd_bwd(const double *A, int batch, int n, double *p
     cudaFree(d);
     return st;
 }
+
+// pg_glynn_c64_dev with host pointers: the real and imaginary planes
+// [batch][n][n] in, per_re/per_im[batch] and abs_sum[batch] (nullable)
+// out; 0 <= n <= 32 (n <= 1 on the host).  Device buffers for the call are
+// allocated and freed inside.  Replaces permanent_parallel_complex
+// (perm_parallel_cuda.cu:416-498), host planes in and host values out.
+extern "C" int pg_glynn_c64(const double *Are, const double *Aim, int batch, int n,
+                            double *per_re, double *per_im, double *abs_sum) {
+    using namespace pg;
+    if (batch < 0 || n < 0 || n > 32)
+        return fail(PG_ERANGE, "complex FP64 engine supports 0 <= n <= 32");
+    if (batch == 0) return PG_OK;
+    if (!per_re || !per_im || (n > 0 && (!Are || !Aim))) return fail(PG_EINVAL, "null argument");
+    if (n <= 1) {
+        for (int b = 0; b < batch; b++) {
+            per_re[b] = n == 0 ? 1.0 : Are[b];
+            per_im[b] = n == 0 ? 0.0 : Aim[b];
+            if (abs_sum) abs_sum[b] = n == 0 ? 1.0 : std::hypot(Are[b], Aim[b]);
+        }
+        return PG_OK;
+    }
+    DeviceInfo dev;
+    int st = device_info(&dev);
+    if (st != PG_OK) return st;
+    const size_t na = (size_t)batch * n * n;
+    const size_t bytes = (2 * na + 3 * (size_t)batch) * sizeof(double);
+    double *d = nullptr;
+    PG_CUDA(cudaMalloc(&d, bytes));
+    double *dre = d, *dim = d + na, *dpre = d + 2 * na, *dpim = dpre + batch,
+           *dabs = dpim + batch;
+    cudaError_t e = cudaMemcpy(dre, Are, na * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dim, Aim, na * sizeof(double), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(d);
+        return cuda_fail(e, "cudaMemcpy(A)");
+    }
+    st = pg_glynn_c64_dev(dre, dim, batch, n, dpre, dpim, dabs, nullptr);
+    if (st == PG_OK) {
+        e = cudaMemcpy(per_re, dpre, (size_t)batch * sizeof(double), cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(per_im, dpim, (size_t)batch * sizeof(double), cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess && abs_sum)
+            e = cudaMemcpy(abs_sum, dabs, (size_t)batch * sizeof(double), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) st = cuda_fail(e, "cudaMemcpy(results)");
+    }
+    cudaFree(d);
+    return st;
+}

@@ -55,6 +55,8 @@ SIGNATURES = {
     "pg_necklace_orbit_stats": ([ctypes.c_int, _c_u64p, _c_u64p], ctypes.c_int),
     "pg_glynn_f64_fwd_bwd": ([_c_f64p, ctypes.c_int, ctypes.c_int, _c_f64p, _c_f64p, _c_f64p],
                              ctypes.c_int),
+    "pg_glynn_c64": ([_c_f64p, _c_f64p, ctypes.c_int, ctypes.c_int, _c_f64p, _c_f64p, _c_f64p],
+                     ctypes.c_int),
     "pg_batch_residues": ([_c_i64p, _c_i64p, _c_i32p, ctypes.c_int, _c_u64p, _c_i32p, _c_u64p],
                           ctypes.c_int),
     "pg_permanent_mod3": ([_c_i64p, ctypes.c_int, _c_intp], ctypes.c_int),
@@ -197,6 +199,22 @@ def glynn_f64_fwd_bwd(matrices, want_grad: bool = True):
                                       ptr(grad, ctypes.c_double) if want_grad else None,
                                       ptr(abs_sum, ctypes.c_double)))
     return per, grad, abs_sum
+
+
+def glynn_c64(matrices):
+    """(per[batch] complex128, abs_sum[batch]) for a batch of complex
+    matrices through the host-pointer C entry point."""
+    a = np.asarray(matrices, dtype=np.complex128)
+    re = np.ascontiguousarray(a.real)
+    im = np.ascontiguousarray(a.imag)
+    batch, n = a.shape[0], a.shape[1]
+    per_re = np.zeros(batch, dtype=np.float64)
+    per_im = np.zeros(batch, dtype=np.float64)
+    abs_sum = np.zeros(batch, dtype=np.float64)
+    check(load().pg_glynn_c64(ptr(re, ctypes.c_double), ptr(im, ctypes.c_double), batch, n,
+                              ptr(per_re, ctypes.c_double), ptr(per_im, ctypes.c_double),
+                              ptr(abs_sum, ctypes.c_double)))
+    return per_re + 1j * per_im, abs_sum
 
 
 def batch_residues(matrices, moduli_lists) -> list[list[int]]:

@@ -40,3 +40,16 @@ def test_batch_residues_mixed_batch(lib):
     got = lib.batch_residues(mats, mods)
     for m, ms, row in zip(mats, mods, got):
         assert row == [oracle.permanent_mod_p(m, q, 4) for q in ms], m.shape
+
+
+def test_c64_host_entry_matches_oracle(lib):
+    rng = np.random.default_rng(63)
+    for n in (2, 6, 11, 14):
+        a = (rng.normal(0, 1 / np.sqrt(n), (3, n, n))
+             + 1j * rng.normal(0, 1 / np.sqrt(n), (3, n, n)))
+        per, s = lib.glynn_c64(a)
+        for b in range(3):
+            want, _ = oracle.glynn_c64(a[b])
+            assert abs(per[b] - want) <= TOL * s[b]
+    per, s = lib.glynn_c64(np.array([[[2.5 - 1j]], [[-1.0 + 3j]]]))
+    assert per.tolist() == [2.5 - 1j, -1.0 + 3j]
