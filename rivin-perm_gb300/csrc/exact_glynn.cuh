@@ -100,24 +100,33 @@ struct ExactShape {
     static constexpr int NR = NG > 1 ? NG - 1 : 1;       // words of the leading product
 };
 
-// Float rows (F, groups of G = 4, N a multiple of 4): in every group the
-// first three row sums are kept as exact FP32 values (the host checks
-// |s| < 2^24 and a bound product below 2^22 for the three), their product
-// is formed by two FMULs on the otherwise idle FP32 pipes, made an integer
-// by adding 1.5 * 2^23 (the low mantissa bits of the sum are then the
-// integer plus 2^22) and finished by one IMUL with the fourth, integer row:
-// one IMAD-pipe instruction per group instead of three.  Table entries and
-// initial sums of those rows hold FP32 bit patterns.
-__host__ __device__ constexpr bool exact_float_row(bool F, int i) { return F && (i & 3) != 3; }
+// Float rows (FR > 0): in every group the first min(FR, size - 1) row sums
+// are kept as exact FP32 values (the host orders each group by bound and
+// checks |s| < 2^24 and a bound product below 2^22 for them).  Their
+// product is formed by FMULs on the otherwise idle FP32 pipes, made an
+// integer by adding 1.5 * 2^23 (the low mantissa bits of the sum are then
+// the integer plus 2^22) and finished by IMULs with the group's integer
+// rows: for groups of 4 with 3 float rows one IMAD-pipe instruction per
+// group instead of three.  Table entries and initial sums of the float rows
+// hold FP32 bit patterns.  The compiled shapes are listed in exact_frows.cu.
+__host__ __device__ constexpr int exact_group_size(int N, int G, int g) {
+    return N - g * G < G ? N - g * G : G;
+}
+__host__ __device__ constexpr int exact_float_rows(int N, int G, int FR, int g) {
+    return FR <= 0 ? 0 : FR < exact_group_size(N, G, g) - 1 ? FR : exact_group_size(N, G, g) - 1;
+}
+__host__ __device__ constexpr bool exact_float_row(int N, int G, int FR, int i) {
+    return i % G < exact_float_rows(N, G, FR, i / G);
+}
 
-template <bool F>
+template <int N, int G, int FR>
 __device__ __forceinline__ int32_t exact_row_add(int i, int32_t s, int32_t d) {
-    if (exact_float_row(F, i)) return __float_as_int(__int_as_float(s) + __int_as_float(d));
+    if (exact_float_row(N, G, FR, i)) return __float_as_int(__int_as_float(s) + __int_as_float(d));
     return s + d;
 }
 
 // Row sums of Gray state `start`: init - sum_{j in gray(start)} 2 a_j.
-template <int N, bool F = false>
+template <int N, int G = 1, int FR = 0>
 __device__ __forceinline__ void exact_init(const int32_t *tab, const int32_t *init,
                                            int32_t *s, uint64_t start) {
     constexpr int NP = (N + 3) & ~3;
@@ -128,7 +137,7 @@ __device__ __forceinline__ void exact_init(const int32_t *tab, const int32_t *in
         if ((gs >> j) & 1) {
             const int32_t *col = tab + (2 * j + 1) * NP;
 #pragma unroll
-            for (int i = 0; i < N; i++) s[i] = exact_row_add<F>(i, s[i], col[i]);
+            for (int i = 0; i < N; i++) s[i] = exact_row_add<N, G, FR>(i, s[i], col[i]);
         }
     }
 }
@@ -185,19 +194,24 @@ struct ProdChainS<END, END> {
     static __device__ __forceinline__ void run(uint32_t *, const int32_t *) {}
 };
 
-template <int N, int G, bool F = false>
+template <int N, int G, int FR = 0>
 __device__ __forceinline__ void exact_term_col(const int32_t *s, uint64_t *col, int64_t &colt,
                                                uint32_t odd, bool first) {
     using S = ExactShape<N, G>;
     constexpr int NG = S::NG, NR = S::NR;
-    static_assert(!F || (G == 4 && N % 4 == 0), "float rows need full groups of 4");
     int32_t x[NG];
 #pragma unroll
     for (int g = 0; g < NG; g++) {
-        if constexpr (F) {
-            const float t = __int_as_float(s[4 * g]) * __int_as_float(s[4 * g + 1]) *
-                            __int_as_float(s[4 * g + 2]);
-            x[g] = (__float_as_int(t + 12582912.0f) - 0x4B400000) * s[4 * g + 3];
+        const int nf = exact_float_rows(N, G, FR, g), sz = exact_group_size(N, G, g);
+        if (nf > 0) {
+            float t = __int_as_float(s[g * G]);
+#pragma unroll
+            for (int u = 1; u < G; u++)
+                if (u < nf) t *= __int_as_float(s[g * G + u]);
+            x[g] = __float_as_int(t + 12582912.0f) - 0x4B400000;
+#pragma unroll
+            for (int u = 1; u < G; u++)
+                if (u >= nf && u < sz) x[g] *= s[g * G + u];
         } else {
             x[g] = s[g * G];
 #pragma unroll
@@ -224,13 +238,13 @@ __device__ __forceinline__ void exact_term_col(const int32_t *s, uint64_t *col, 
 
 // Walk chunks [c_begin, c_end) (row sums s already at state c_begin*2^log_len)
 // adding every term into acc.  Returns false if the abort word was seen.
-template <int N, int G, bool F = false>
+template <int N, int G, int FR = 0>
 __device__ __forceinline__ bool exact_walk(const int32_t *tab, int32_t *s, uint32_t *acc,
                                            uint64_t c_begin, uint64_t c_end, int log_len,
                                            volatile const int *abort_flag) {
     using S = ExactShape<N, G>;
     constexpr int NP = S::NP, LOGU = S::LOGU, U = 1 << LOGU;
-    static_assert(!F || EXACT_COLACC, "float rows need the column form of the term");
+    static_assert(FR == 0 || EXACT_COLACC, "float rows need the column form of the term");
     const uint32_t Q = (1u << log_len) >> LOGU;
 #if EXACT_COLACC
     uint64_t col[S::NR > 1 ? S::NR - 1 : 1];
@@ -265,15 +279,15 @@ __device__ __forceinline__ bool exact_walk(const int32_t *tab, int32_t *s, uint3
 #pragma unroll
                     for (int v = 0; v < NP / 4; v++) {
                         const int4 d = col[v];
-                        if (4 * v + 0 < N) s[4 * v + 0] = exact_row_add<F>(4 * v + 0, s[4 * v + 0], d.x);
-                        if (4 * v + 1 < N) s[4 * v + 1] = exact_row_add<F>(4 * v + 1, s[4 * v + 1], d.y);
-                        if (4 * v + 2 < N) s[4 * v + 2] = exact_row_add<F>(4 * v + 2, s[4 * v + 2], d.z);
-                        if (4 * v + 3 < N) s[4 * v + 3] = exact_row_add<F>(4 * v + 3, s[4 * v + 3], d.w);
+                        if (4 * v + 0 < N) s[4 * v + 0] = exact_row_add<N, G, FR>(4 * v + 0, s[4 * v + 0], d.x);
+                        if (4 * v + 1 < N) s[4 * v + 1] = exact_row_add<N, G, FR>(4 * v + 1, s[4 * v + 1], d.y);
+                        if (4 * v + 2 < N) s[4 * v + 2] = exact_row_add<N, G, FR>(4 * v + 2, s[4 * v + 2], d.z);
+                        if (4 * v + 3 < N) s[4 * v + 3] = exact_row_add<N, G, FR>(4 * v + 3, s[4 * v + 3], d.w);
                     }
                 }
                 // chunks start at even states, so (-1)^g = (-1)^r
 #if EXACT_COLACC
-                exact_term_col<N, G, F>(s, col, colt, (uint32_t)(r & 1), r == 0);
+                exact_term_col<N, G, FR>(s, col, colt, (uint32_t)(r & 1), r == 0);
 #else
                 exact_term<N, G>(s, acc, (uint32_t)(r & 1));
 #endif
@@ -307,7 +321,7 @@ __host__ __device__ constexpr int exact_min_blocks(int N) {
            : (65536 / (256 * (N + 64)));
 }
 
-template <int N, int G, bool F = false>
+template <int N, int G, int FR = 0>
 __global__ void __launch_bounds__(256, exact_min_blocks(N))
 exact_glynn_kernel(ExactArgs a) {
     using S = ExactShape<N, G>;
@@ -330,8 +344,8 @@ exact_glynn_kernel(ExactArgs a) {
     bool aborted = false;
     if (c_begin < c_end) {
         int32_t s[N];
-        exact_init<N, F>(tab, a.init, s, c_begin << a.log_len);
-        aborted = !exact_walk<N, G, F>(tab, s, acc, c_begin, c_end, a.log_len, a.abort_flag);
+        exact_init<N, G, FR>(tab, a.init, s, c_begin << a.log_len);
+        aborted = !exact_walk<N, G, FR>(tab, s, acc, c_begin, c_end, a.log_len, a.abort_flag);
     }
 
     // Block reduction: word l < NL-1 contributes acc[l] (unsigned), the top
@@ -358,30 +372,30 @@ exact_glynn_kernel(ExactArgs a) {
     if (threadIdx.x == 0 && any_abort) atomicExch(a.status, 1);
 }
 
-template <int N, int G, bool F = false>
+template <int N, int G, int FR = 0>
 cudaError_t launch_exact_glynn(const ExactArgs &args, int blocks,
                                cudaStream_t stream) {
     constexpr int NP = ExactShape<N, G>::NP;
     const size_t smem = (size_t)(N - 1) * 2 * NP * sizeof(int32_t);
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(
-            exact_glynn_kernel<N, G, F>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            exact_glynn_kernel<N, G, FR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
             (int)smem);
         if (e != cudaSuccess) return e;
     }
-    exact_glynn_kernel<N, G, F><<<blocks, 256, smem, stream>>>(args);
+    exact_glynn_kernel<N, G, FR><<<blocks, 256, smem, stream>>>(args);
     return cudaGetLastError();
 }
 
-template <int N, int G, bool F = false>
+template <int N, int G, int FR = 0>
 int occupancy_exact_glynn() {
     constexpr int NP = ExactShape<N, G>::NP;
     const size_t smem = (size_t)(N - 1) * 2 * NP * sizeof(int32_t);
     if (smem > 48 * 1024)
-        cudaFuncSetAttribute(exact_glynn_kernel<N, G, F>,
+        cudaFuncSetAttribute(exact_glynn_kernel<N, G, FR>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, exact_glynn_kernel<N, G, F>,
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, exact_glynn_kernel<N, G, FR>,
                                                       256, smem) != cudaSuccess)
         return 1;
     return nb < 1 ? 1 : nb;
@@ -390,11 +404,17 @@ int occupancy_exact_glynn() {
 // Largest compiled group size (gen_exact_inst.py); hosts try G from here down.
 constexpr int EXACT_MAX_G = 10;
 
-// Float-row form (exact_float_row): 1 lets the host take it for the orders
-// pg_exact.cu compiles it for when a matrix's bounds allow.
+// Float-row form (exact_float_row): 1 lets the host take it for the shapes
+// exact_frows.cu compiles when a matrix's bounds allow.
 #ifndef EXACT_FROWS
 #define EXACT_FROWS 1
 #endif
+
+// Largest compiled float-row count for (N, G), 0 when none (exact_frows.cu).
+int exact_frows_max(int N, int G);
+cudaError_t launch_exact_frows(int N, int G, int FR, const ExactArgs &args, int blocks,
+                               cudaStream_t stream);
+int occupancy_exact_frows(int N, int G, int FR);
 
 // Compiled (N, G) pairs; returns cudaErrorInvalidValue / 0 when absent.
 cudaError_t launch_exact_any(int N, int G, const ExactArgs &args, int blocks,

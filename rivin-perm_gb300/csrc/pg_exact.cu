@@ -105,49 +105,14 @@ static void add_i64_at(std::vector<uint32_t> &w, int pos, long long v) {
 
 
 // Everything one exact evaluation needs, built once on the host.
-// Orders with the float-row form of the kernel (exact_float_row): G = 4.
-// (At order 36 it spills and is slower than the integer form.)
-#define PG_EXACT_FROWS_ORDERS(X) X(24) X(28) X(32)
-
-static bool frows_compiled(int n) {
-    switch (n) {
-#define PG_FR_YES(NN) case NN:
-        PG_EXACT_FROWS_ORDERS(PG_FR_YES)
-#undef PG_FR_YES
-        return EXACT_FROWS != 0;
-    default:
-        return false;
-    }
-}
-
-static cudaError_t launch_exact_frows(int n, const ExactArgs &args, int blocks,
-                                      cudaStream_t stream) {
-    switch (n) {
-#define PG_FR_LAUNCH(NN) case NN: return launch_exact_glynn<NN, 4, true>(args, blocks, stream);
-        PG_EXACT_FROWS_ORDERS(PG_FR_LAUNCH)
-#undef PG_FR_LAUNCH
-    default:
-        return cudaErrorInvalidValue;
-    }
-}
-
-static int occupancy_exact_frows(int n) {
-    switch (n) {
-#define PG_FR_OCC(NN) case NN: return occupancy_exact_glynn<NN, 4, true>();
-        PG_EXACT_FROWS_ORDERS(PG_FR_OCC)
-#undef PG_FR_OCC
-    default:
-        return 1;
-    }
-}
-
-// Float rows for a grouping in groups of 4: within each group the row of
-// largest bound goes last (the integer row) and the other three must have
-// bounds below 2^24 (exact FP32 sums) with a product below 2^22 (exact
+// Float rows for group size G: within each group the rows are ordered by
+// increasing bound, and the first exact_float_rows(n, G, FR, g) of them must
+// have bounds below 2^24 (exact FP32 sums) with a product below 2^22 (exact
 // FP32 product, converted by the 1.5 * 2^23 add).  Reorders `order` in
-// place and returns true when every group qualifies.
-static bool frows_arrange(const int64_t *A, int n, std::vector<int> *order) {
-    if (n % 4 || !frows_compiled(n)) return false;
+// place (group membership is unchanged) and returns true when every group
+// qualifies.
+static bool frows_arrange(const int64_t *A, int n, int G, int FR, std::vector<int> *order) {
+    if (FR <= 0) return false;
     std::vector<uint64_t> B(n);
     for (int i = 0; i < n; i++) {
         uint64_t s = 0;
@@ -158,11 +123,13 @@ static bool frows_arrange(const int64_t *A, int n, std::vector<int> *order) {
         B[i] = s;
     }
     std::vector<int> o = *order;
-    for (int g = 0; g < n / 4; g++) {
-        int *grp = o.data() + 4 * g;
-        std::sort(grp, grp + 4, [&](int x, int y) { return B[x] < B[y]; });
+    const int NG = (n + G - 1) / G;
+    for (int g = 0; g < NG; g++) {
+        const int sz = exact_group_size(n, G, g), nf = exact_float_rows(n, G, FR, g);
+        int *grp = o.data() + g * G;
+        std::sort(grp, grp + sz, [&](int x, int y) { return B[x] < B[y]; });
         unsigned __int128 prod = 1;
-        for (int t = 0; t < 3; t++) {
+        for (int t = 0; t < nf; t++) {
             if (B[grp[t]] >= (1ull << 24)) return false;
             prod *= (B[grp[t]] ? B[grp[t]] : 1);
         }
@@ -181,7 +148,7 @@ static uint32_t float_bits(int64_t v) {
 
 struct ExactPlan {
     int n = 0, G = 0, NG = 0, NL = 0, need_bits = 0;
-    bool frows = false;          // float-row form of the kernel
+    int fr = 0;                  // float rows per group (0: integer rows)
     ChunkPlan chunks{};
     uint64_t chunk0 = 0;
     uint64_t blocks = 0;
@@ -205,7 +172,8 @@ static int plan_build(const int64_t *A, int n, ExactPlan *P) {
     st = abort_flag_device(&P->abort_dev);
     if (st != PG_OK) return st;
     const int N = n, NCOL = n - 1, NP = (n + 3) & ~3;
-    P->frows = G == 4 && frows_arrange(A, n, &order);
+    const int fr_max = exact_frows_max(n, G);
+    P->fr = frows_arrange(A, n, G, fr_max, &order) ? fr_max : 0;
     P->n = n;
     P->G = G;
     P->NG = (N + G - 1) / G;
@@ -220,7 +188,7 @@ static int plan_build(const int64_t *A, int n, ExactPlan *P) {
     int32_t *init = (int32_t *)(P->image.data() + off_init);
     for (int ii = 0; ii < N; ii++) {
         const int64_t *row = A + (size_t)order[ii] * n;
-        const bool fl = P->frows && exact_float_row(true, ii);
+        const bool fl = P->fr > 0 && exact_float_row(N, G, P->fr, ii);
         const auto enc = [&](int64_t v) { return fl ? (int32_t)float_bits(v) : (int32_t)v; };
         int64_t sum = 0;
         for (int j = 0; j < n; j++) sum += row[j];
@@ -233,7 +201,7 @@ static int plan_build(const int64_t *A, int n, ExactPlan *P) {
     // One resident wave of blocks (occupancy-limited), each thread owning a
     // contiguous range of ~128 chunks of >= 64 states; small orders use
     // fewer blocks so every thread still gets >= 512 states.
-    const int occ = P->frows ? occupancy_exact_frows(N) : occupancy_exact_any(N, G);
+    const int occ = P->fr ? occupancy_exact_frows(N, G, P->fr) : occupancy_exact_any(N, G);
     const int log_states = n - 1;
     uint64_t blocks = (uint64_t)occ * dev.sm_count;
     while (blocks > 1 && ((1ull << log_states) >> 9) < blocks * 256) blocks >>= 1;
@@ -270,8 +238,8 @@ static int plan_launch(ExactPlan *P, cudaStream_t stream) {
     args.log_len = P->chunks.log_len;
     args.chunk0 = P->chunk0;
     PG_CUDA(cudaMemsetAsync(P->dev + P->off_acc, 0, P->total - P->off_acc, stream));
-    PG_CUDA(P->frows ? launch_exact_frows(P->n, args, (int)P->blocks, stream)
-                     : launch_exact_any(P->n, P->G, args, (int)P->blocks, stream));
+    PG_CUDA(P->fr ? launch_exact_frows(P->n, P->G, P->fr, args, (int)P->blocks, stream)
+                  : launch_exact_any(P->n, P->G, args, (int)P->blocks, stream));
     return PG_OK;
 }
 
@@ -443,8 +411,8 @@ int pg_exact_plan_info(const pg_exact_plan *plan, int *group, int *words,
     if (group) *group = P.G;
     if (words) *words = P.NG;
     if (states) *states = 1ull << (P.n - 1);
-    // the algorithm's row-group multiplies (with float rows two of every
-    // three run as exact FP32 multiplies on the FP32 pipe)
+    // the algorithm's row-group multiplies (with float rows most of them
+    // run as exact FP32 multiplies on the FP32 pipe)
     if (imul_per_state) *imul_per_state = (uint64_t)(P.n - P.NG);
     if (imad_wide_per_state) *imad_wide_per_state = (uint64_t)P.NG * (P.NG - 1) / 2;
     return PG_OK;

@@ -50,7 +50,8 @@ def test_exact_instantiations_match_their_generator(tmp_path):
     gen = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(gen)
     gen.main()
-    made = sorted(p.name for p in tmp_path.glob("exact_*.cu"))
-    assert made == sorted(p.name for p in csrc.glob("exact_*.cu"))
+    generated = ("exact_inst_*.cu", "exact_dispatch.cu")
+    made = sorted(p.name for pat in generated for p in tmp_path.glob(pat))
+    assert made == sorted(p.name for pat in generated for p in csrc.glob(pat))
     for name in made:
         assert (tmp_path / name).read_text() == (csrc / name).read_text(), name
