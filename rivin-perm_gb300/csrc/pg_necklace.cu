@@ -499,8 +499,18 @@ struct NkQueue {
 constexpr int NK_QUEUE = 4;        // accepted words a lane may hold
 constexpr int NK_WALK_STEPS = 3;   // walker steps per evaluation (about 2.5 steps per word)
 
+// Resident blocks per SM requested from ptxas for orders up to 42: three
+// (80 registers, a few bytes of spill) beat two by 4-11 % on S_37..S_43,
+// the walk's latency being hidden by more warps.  0: no request.
+#ifndef PG_NK_MIN_BLOCKS
+#define PG_NK_MIN_BLOCKS 3
+#endif
+__host__ __device__ constexpr int nk_min_blocks(int L) {
+    return PG_NK_MIN_BLOCKS > 0 && L <= 42 ? PG_NK_MIN_BLOCKS : 1;
+}
+
 template <int L, bool W>
-__global__ void __launch_bounds__(256) necklace_m32_kernel(NeckArgs a) {
+__global__ void __launch_bounds__(256, nk_min_blocks(L)) necklace_m32_kernel(NeckArgs a) {
     constexpr int LS = nk_stride(L);
     extern __shared__ uint4 nsm[];
     const int k = blockIdx.y;
