@@ -2,7 +2,12 @@
 """Benchmark: Glynn steps/s and time-to-exact for per(A), A 32x32 int.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload generic32|generic24]
+                    [--workload generic32|generic24|batch4096|float28|schur|schur41|
+                                binary40|grid40|rook28|mod3_40] [--no-cpu]
+
+The default workload is generic32 (below); the others print their own
+metric line (batched exact permanents, FP64 forward+gradient, Schur
+permanents, binary matrices, rook polynomial, permanent mod 3).
 
 One step = one exact evaluation of per(A) for the seeded workload matrix:
 the full 2^(n-1) Gray traversal.  `value` is Glynn steps per second toward
