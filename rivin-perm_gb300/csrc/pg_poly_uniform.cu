@@ -3,8 +3,8 @@
 // With every row of C equal, every row's constant part is the same
 // c(d) = sum_j d_j c_j, so
 //   prod_i (c + x l_i(d)) = sum_k e_k(l_1(d), ..., l_n(d)) c^(n-k) x^k
-// with e_k the elementary symmetric sums (the weighting of
-// perm_polynomial.py:1288-1411 by powers of the common part).  A state
+// with e_k the elementary symmetric sums (the reference's rook_polynomial,
+// perm_polynomial.py:1288-1411, is per(J + x A): C = J).  A state
 // costs the e_k recurrence, E[d] += l_r E[d-1] with ONE Montgomery product
 // per coefficient (the general kernel needs a two-product reduction), and
 // 2n - 1 products for the powers of c and the weighting.  Only one copy of
