@@ -125,3 +125,22 @@ def test_sharded_partials_combine_to_exact(lib, world):
     want = int(golden("exact_generic.json")["cases"][-1]["permanent"])
     words = [shard.exact_partial_words(a, *shard.state_range(24, r, world)) for r in range(world)]
     assert shard.combine_exact_words(words, 24) == want
+
+
+@pytest.mark.parametrize("n", [40, 44, 48])
+@pytest.mark.parametrize("kind", ["int", "binary"])
+def test_exact_partial_windows_at_the_largest_orders(lib, n, kind):
+    # a whole traversal at these orders takes minutes to hours; windows of
+    # 2^22 Gray states at the start, the middle and the end check the exact
+    # kernel's widest shapes (groups up to 10, two extra accumulator words)
+    # against the oracle's unscaled range sum modulo two primes
+    from permgpu import shard
+    rng = np.random.default_rng(800 + n + (kind == "binary"))
+    a = (rng.integers(-8, 9, (n, n)) if kind == "int"
+         else (rng.random((n, n)) < 0.5).astype(np.int64))
+    assert lib.exact_supported(a)
+    states, w = 1 << (n - 1), 1 << 22
+    for lo in (0, states // 2 + (1 << 24), states - w):
+        v = shard.words_value(shard.exact_partial_words(a, lo, lo + w))
+        for p in (2_147_483_647, 1_000_000_007):
+            assert v % p == oracle.glynn_range_mod_p(a, p, lo, lo + w), (n, kind, lo, p)
