@@ -67,6 +67,18 @@ int pg_residues(const int64_t *A, int n, const uint64_t *moduli, int k,
                 uint64_t *out);
 
 /*
+ * Sharded residues: out[t] = the unscaled Glynn sum over Gray states
+ * [state_lo, state_hi) (both even, lo < hi <= 2^(n-1)) mod moduli[t], i.e.
+ * without the 2^(1-n) factor, for odd moduli 3 <= m < 2^32 and 2 <= n < 64.
+ * Summing the values of a partition of [0, 2^(n-1)) mod m and multiplying
+ * by 2^(1-n) gives per(A) mod m (permgpu.shard.combine_residues), so ranks
+ * can split one modulus's traversal.  The reference's OpenMP loop splits
+ * the same Gray walk across threads (perm_c_omp.c:556-639).
+ */
+int pg_residues_partial(const int64_t *A, int n, uint64_t state_lo, uint64_t state_hi,
+                        const uint64_t *moduli, int k, uint64_t *out);
+
+/*
  * Schur residues: out[t] = perm(S_n) mod primes[t] with S_n[j][c] =
  * omegas[t]^(j*c).  For odd n, odd p and omega^n == 1 this evaluates
  * n * per(minor) with the (n-1)x(n-1) minor omega^((r+1)(c+1)); otherwise

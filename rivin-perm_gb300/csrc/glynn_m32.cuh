@@ -34,8 +34,9 @@ struct M32Args {
     unsigned long long *acc;   // [k]  zeroed by the host
     int *status;               // set to 1 when the abort flag stopped the launch
     volatile const int *abort_flag;
-    uint64_t chunks;           // chunks per modulus
+    uint64_t chunks;           // chunks per modulus: [chunk0, chunk0 + chunks)
     int log_len;               // chunk length 2^log_len, LOGU <= log_len <= 30
+    uint64_t chunk0;           // first chunk (0 for a whole traversal)
 };
 
 __device__ __forceinline__ uint32_t m32_redc_mul(uint32_t a, uint32_t b,
@@ -117,8 +118,8 @@ glynn_m32_kernel(M32Args a) {
     // initialise once, cross chunk boundaries with an ordinary Gray step.
     const uint64_t T = (uint64_t)gridDim.x * blockDim.x;
     const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const uint64_t c_begin = tid * a.chunks / T;
-    const uint64_t c_end = (tid + 1) * a.chunks / T;
+    const uint64_t c_begin = a.chunk0 + tid * a.chunks / T;
+    const uint64_t c_end = a.chunk0 + (tid + 1) * a.chunks / T;
 
     uint32_t s[N];
     if (c_begin < c_end) {

@@ -155,13 +155,16 @@ static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 // per(mats[t]) mod moduli[t] for odd moduli 3 <= m < 2^31, or for odd
 // 2^31 <= m < 2^32 with `wide` (fully reduced form of the same kernel), n >= 2.
+// With hi > 0, out[t] is instead the unscaled Glynn sum over Gray states
+// [lo, hi) mod moduli[t] (no 2^(1-n) factor); lo and hi are multiples of 2.
 static int glynn_m32_batch(const uint64_t *mats, int n, const uint64_t *moduli,
-                           int k, bool wide, uint64_t *out) {
+                           int k, bool wide, uint64_t *out, uint64_t lo = 0,
+                           uint64_t hi = 0) {
     if (k > 65535) {   // grid.y limit: split into launches of <= 65535 moduli
         for (int t0 = 0; t0 < k; t0 += 65535) {
             const int kk = k - t0 < 65535 ? k - t0 : 65535;
             int st = glynn_m32_batch(mats + (size_t)t0 * n * n, n, moduli + t0, kk, wide,
-                                     out + t0);
+                                     out + t0, lo, hi);
             if (st != PG_OK) return st;
         }
         return PG_OK;
@@ -224,8 +227,10 @@ static int glynn_m32_batch(const uint64_t *mats, int n, const uint64_t *moduli,
     // orders use fewer blocks so every thread keeps >= 512 states).
     const int occ = occupancy_m32_any(N, wide);
     const int log_states = n - 1;
+    const bool partial = hi > 0;
+    const uint64_t span = partial ? hi - lo : 1ull << log_states;
     uint64_t bpm = ((uint64_t)occ * dev.sm_count + k - 1) / k;
-    while (bpm > 1 && ((1ull << log_states) >> 9) < bpm * 256) bpm >>= 1;
+    while (bpm > 1 && (span >> 9) < bpm * 256) bpm >>= 1;
     if (bpm < 1) bpm = 1;
     if (bpm > 65535) bpm = 65535;
     int log_T = 0;
@@ -238,6 +243,21 @@ static int glynn_m32_batch(const uint64_t *mats, int n, const uint64_t *moduli,
     if (pl.log_len < 1) pl.log_len = 1;
     pl.chunks = 1ull << (log_states - pl.log_len);
 
+    uint64_t chunk0 = 0;
+    if (partial) {
+        // about 128 chunks per thread over the window, shortened until the
+        // chunk length divides lo and hi; the kernel steps 2 states per
+        // iteration
+        int log_span = 0;
+        while ((2ull << log_span) <= span) log_span++;
+        int ll = log_span - (log_T + 7);
+        if (ll > 30) ll = 30;
+        if (ll < 1) ll = 1;
+        while (ll > 1 && ((lo | hi) & ((1ull << ll) - 1))) ll--;
+        pl.log_len = ll;
+        pl.chunks = span >> ll;
+        chunk0 = lo >> ll;
+    }
     M32Args args;
     args.tabs = (const uint32_t *)(d + off_tab);
     args.init = (const uint32_t *)(d + off_init);
@@ -248,6 +268,7 @@ static int glynn_m32_batch(const uint64_t *mats, int n, const uint64_t *moduli,
     args.abort_flag = abort_dev;
     args.chunks = pl.chunks;
     args.log_len = pl.log_len;
+    args.chunk0 = chunk0;
 
     PG_CUDA(cudaMemcpyAsync(d, h, off_acc, cudaMemcpyHostToDevice, ws->stream));
     PG_CUDA(cudaMemsetAsync(d + off_acc, 0, total - off_acc, ws->stream));
@@ -265,7 +286,7 @@ static int glynn_m32_batch(const uint64_t *mats, int n, const uint64_t *moduli,
         const uint64_t inv2 = (p >> 1) + 1;
         uint64_t r = acc[t] % p;
         r = mulmod_u64(r, powmod_u64(R, (uint64_t)(n - 1), p), p);
-        r = mulmod_u64(r, powmod_u64(inv2, (uint64_t)(n - 1), p), p);
+        if (!partial) r = mulmod_u64(r, powmod_u64(inv2, (uint64_t)(n - 1), p), p);
         out[t] = r;
     }
     return PG_OK;
@@ -512,6 +533,41 @@ int pg_residues(const int64_t *A, int n, const uint64_t *moduli, int k,
     if (st != PG_OK) return st;
     if (k == 0) return PG_OK;
     return residues_impl(A, n, moduli, k, out);
+}
+
+int pg_residues_partial(const int64_t *A, int n, uint64_t state_lo, uint64_t state_hi,
+                        const uint64_t *moduli, int k, uint64_t *out) {
+    using namespace pg;
+    if (n < 2 || n >= 64) return fail(PG_ERANGE, "partial residues need 2 <= n < 64");
+    if (!A) return fail(PG_EINVAL, "matrix is null");
+    if (k > 0 && (!moduli || !out)) return fail(PG_EINVAL, "null argument");
+    const uint64_t states = 1ull << (n - 1);
+    if (state_lo >= state_hi || state_hi > states)
+        return fail(PG_ERANGE, "state range must satisfy lo < hi <= 2^(n-1)");
+    if ((state_lo | state_hi) & 1) return fail(PG_EINVAL, "state range bounds must be even");
+    for (int t = 0; t < k; t++)
+        if (moduli[t] < 3 || !(moduli[t] & 1) || moduli[t] >= (1ull << 32))
+            return fail(PG_ERANGE, "partial residues need odd moduli 3 <= m < 2^32");
+    const size_t nn = (size_t)n * n;
+    for (int wide = 0; wide < 2; wide++) {
+        std::vector<uint64_t> mats, mods;
+        std::vector<int> idx;
+        for (int t = 0; t < k; t++) {
+            if ((moduli[t] >= (1ull << 31)) != (wide == 1)) continue;
+            const size_t base = mats.size();
+            mats.resize(base + nn);
+            for (size_t i = 0; i < nn; i++) mats[base + i] = normmod_i64(A[i], moduli[t]);
+            mods.push_back(moduli[t]);
+            idx.push_back(t);
+        }
+        if (idx.empty()) continue;
+        std::vector<uint64_t> res(idx.size());
+        const int st = glynn_m32_batch(mats.data(), n, mods.data(), (int)idx.size(), wide == 1,
+                                       res.data(), state_lo, state_hi);
+        if (st != PG_OK) return st;
+        for (size_t q = 0; q < idx.size(); q++) out[idx[q]] = res[q];
+    }
+    return PG_OK;
 }
 
 int pg_schur_residues(int n, const uint64_t *primes, const uint64_t *omegas,

@@ -49,6 +49,8 @@ SIGNATURES = {
     "pg_abort": ([], None),
     "pg_clear_abort": ([], None),
     "pg_residues": ([_c_i64p, ctypes.c_int, _c_u64p, ctypes.c_int, _c_u64p], ctypes.c_int),
+    "pg_residues_partial": ([_c_i64p, ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64, _c_u64p,
+                             ctypes.c_int, _c_u64p], ctypes.c_int),
     "pg_schur_residues": ([ctypes.c_int, _c_u64p, _c_u64p, ctypes.c_int, _c_u64p], ctypes.c_int),
     "pg_schur_residues_method": ([ctypes.c_int, _c_u64p, _c_u64p, ctypes.c_int, ctypes.c_int,
                                   _c_u64p], ctypes.c_int),

@@ -63,6 +63,20 @@ def combine_exact_words(word_lists: Iterable[Sequence[int]], n: int) -> int:
     return total >> max(n - 1, 0)
 
 
+def residue_partials(matrix, lo: int, hi: int, moduli: Sequence[int]) -> List[int]:
+    """Unscaled Glynn sums over Gray states [lo, hi) modulo each odd modulus
+    below 2^32 (pg_residues_partial); combine_residues turns the values of a
+    partition of [0, 2^(n-1)) into per(A) mod p."""
+    a = np.ascontiguousarray(matrix, dtype=np.int64)
+    mods = np.ascontiguousarray([int(m) for m in moduli], dtype=np.uint64)
+    out = np.zeros(len(mods), dtype=np.uint64)
+    _lib.check(_lib.load().pg_residues_partial(_lib.ptr(a, ctypes.c_int64), a.shape[0],
+                                               ctypes.c_uint64(lo), ctypes.c_uint64(hi),
+                                               _lib.ptr(mods, ctypes.c_uint64), len(mods),
+                                               _lib.ptr(out, ctypes.c_uint64)))
+    return [int(x) for x in out]
+
+
 def combine_residues(partials: Iterable[int], p: int, n: int) -> int:
     """per(A) mod odd p from unscaled partial Glynn sums mod p."""
     total = sum(int(x) for x in partials) % p
