@@ -174,3 +174,35 @@ def test_schur_necklace_method_rejects_unsupported_inputs():
         _lib.schur_residues(11, [23], [5], method="necklace")                  # 5^11 != 1 mod 23
     with pytest.raises(ValueError):
         _lib.schur_residues(11, [23], [1], method="ryser")
+
+
+def test_partial_residue_arguments_are_checked_on_the_host():
+    # pg_residues_partial validates before any device call
+    from permgpu import _lib, shard
+    a = np.arange(16, dtype=np.int64).reshape(4, 4)
+    for lo, hi, mods, code in [
+            (1, 4, [1_000_003], "PG_EINVAL"),          # odd bound
+            (4, 4, [1_000_003], "PG_ERANGE"),          # empty range
+            (0, 16, [1_000_003], "PG_ERANGE"),         # beyond 2^(n-1) = 8
+            (0, 4, [1 << 32], "PG_ERANGE"),            # modulus >= 2^32
+            (0, 4, [4], "PG_ERANGE"),                  # even modulus
+    ]:
+        with pytest.raises(_lib.PermGpuError, match=code):
+            shard.residue_partials(a, lo, hi, mods)
+    with pytest.raises(_lib.PermGpuError, match="PG_ERANGE"):
+        shard.residue_partials(np.ones((1, 1), dtype=np.int64), 0, 1, [7])   # n < 2
+
+
+def test_fp64_entries_handle_orders_below_two_on_the_host():
+    # n = 0 and n = 1 are answered without a device, like the reference's
+    # empty-matrix and 1x1 conventions
+    from permgpu import _lib
+    per, grad, s = _lib.glynn_f64_fwd_bwd(np.array([[[2.5]], [[-1.0]]]))
+    assert per.tolist() == [2.5, -1.0] and grad.ravel().tolist() == [1.0, 1.0]
+    assert s.tolist() == [2.5, 1.0]
+    per, s = _lib.glynn_c64(np.array([[[2.5 - 1j]], [[3j]]]))
+    assert per.tolist() == [2.5 - 1j, 3j] and s[1] == 3.0
+    per, s = _lib.glynn_c64(np.zeros((2, 0, 0), dtype=np.complex128))
+    assert per.tolist() == [1, 1]
+    with pytest.raises(_lib.PermGpuError, match="PG_ERANGE"):
+        _lib.glynn_c64(np.zeros((1, 33, 33), dtype=np.complex128))
