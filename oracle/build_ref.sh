@@ -14,7 +14,8 @@ if [ ! -f "$REF/perm_c_omp.c" ]; then
   echo "reference sources not found under $REF; oracle/_ref not built" >&2
   exit 0
 fi
-mkdir -p "$OUT"
+mkdir -p "$OUT" "$HERE/.tmp"
+export TMPDIR="$HERE/.tmp"      # the compiler's temporary files stay in the tree
 PYINC="$(python3 -c 'import sysconfig; print(sysconfig.get_paths()["include"])')"
 NPINC="$(python3 -c 'import numpy; print(numpy.get_include())')"
 SUFFIX="$(python3 -c 'import sysconfig; print(sysconfig.get_config_var("EXT_SUFFIX"))')"

@@ -37,7 +37,9 @@ def build(force: bool = False) -> Path:
     if force or not LIB.exists() or LIB.stat().st_mtime < src.stat().st_mtime:
         cmd = ["gcc", "-O3", "-fopenmp", "-fPIC", "-shared", "-std=gnu99",
                str(src), "-o", str(LIB), "-lm"]
-        subprocess.run(cmd, check=True)
+        tmp = HERE / ".tmp"           # the compiler's temporary files stay here
+        tmp.mkdir(exist_ok=True)
+        subprocess.run(cmd, check=True, env=dict(os.environ, TMPDIR=str(tmp)))
     return LIB
 
 

@@ -5,10 +5,12 @@
 // s_i(d) = sum_j d_j a_ij fit in int32 and every term prod_i s_i is an exact
 // integer of at most sum_i log2(B_i) bits.  This kernel keeps the row sums
 // exact, multiplies them in groups of G rows with plain 32-bit IMUL (the host
-// permutes rows so that every group's bound product is < 2^31), forms the
-// exact magnitude of the term as an NG-word integer (mul.wide products plus
-// an ALU carry chain), and adds it with its sign into an NL-word
-// two's-complement accumulator.
+// permutes rows so that every group's bound product is < 2^31), folds the
+// term's sign into the first group, forms the signed product of the first
+// NG-1 groups as a multi-word integer (mul.wide products plus an ALU carry
+// chain), and multiplies it by the last group into 64-bit column
+// accumulators that are added into an NL-word two's-complement accumulator
+// every 2^LOGU terms (col_acc.cuh).
 //
 // Versus a CRT residue walk this removes the modular reductions and the
 // per-prime repetition: for n = 32, entries in [-8,8], one exact term costs
@@ -26,30 +28,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#include "acc_chain.cuh"
 #include "col_acc.cuh"
-#include "mp_mul.cuh"
-#include "mp_mul_oop.cuh"
-
-// 1: the last row group multiplies the running product into 64-bit column
-// accumulators folded every 2^LOGU terms (col_acc.cuh); 0: every term is
-// formed in full and added with its sign (acc_chain.cuh).
-#ifndef EXACT_COLACC
-#define EXACT_COLACC 1
-#endif
-
-#ifndef EXACT_MUL_OOP
-#define EXACT_MUL_OOP 0
-#endif
 
 #ifndef EXACT_LOGU
 #define EXACT_LOGU 2
-#endif
-#ifndef EXACT_ACC_PTX
-#define EXACT_ACC_PTX 1
-#endif
-#ifndef EXACT_MUL_PTX
-#define EXACT_MUL_PTX 1
 #endif
 #ifndef EXACT_MIN_BLOCKS
 #define EXACT_MIN_BLOCKS 0
@@ -60,36 +42,6 @@ namespace pg {
 __device__ __forceinline__ constexpr int exact_ctz_small(int r) {
     return (r & 1) ? 0 : (r & 2) ? 1 : (r & 4) ? 2 : (r & 8) ? 3 : 4;
 }
-
-// P[0..NG-1] = prod_{g < NG} mag[g], one word multiply per group (g words
-// times one word, growing the product by one word each time).
-template <int G0, int NG>
-struct ProdChain {
-    static __device__ __forceinline__ void run(uint32_t *P, const uint32_t *mag) {
-#if EXACT_MUL_OOP
-        uint32_t Q[G0 + 1];
-        MulWordOop<G0>::apply(P, Q, mag[G0]);
-#pragma unroll
-        for (int l = 0; l <= G0; l++) P[l] = Q[l];
-#elif EXACT_MUL_PTX
-        MulWord<G0>::apply(P, mag[G0]);
-#else
-        uint32_t carry = 0;
-#pragma unroll
-        for (int l = 0; l < G0; l++) {
-            const uint64_t t = (uint64_t)P[l] * mag[G0] + carry;
-            P[l] = (uint32_t)t;
-            carry = (uint32_t)(t >> 32);
-        }
-        P[G0] = carry;
-#endif
-        ProdChain<G0 + 1, NG>::run(P, mag);
-    }
-};
-template <int NG>
-struct ProdChain<NG, NG> {
-    static __device__ __forceinline__ void run(uint32_t *, const uint32_t *) {}
-};
 
 template <int N, int G>
 struct ExactShape {
@@ -140,42 +92,6 @@ __device__ __forceinline__ void exact_init(const int32_t *tab, const int32_t *in
             for (int i = 0; i < N; i++) s[i] = exact_row_add<N, G, FR>(i, s[i], col[i]);
         }
     }
-}
-
-// One Glynn term at the current row sums: acc += (-1)^(odd + signs) * prod s.
-template <int N, int G>
-__device__ __forceinline__ void exact_term(const int32_t *s, uint32_t *acc, uint32_t odd) {
-    using S = ExactShape<N, G>;
-    constexpr int NG = S::NG, NL = S::NL;
-    // exact group products (|x| < 2^31 by the host's grouping); the sign is
-    // the XOR of the group signs and the Glynn sign
-    uint32_t sx = odd << 31;
-    uint32_t mag[NG];
-#pragma unroll
-    for (int g = 0; g < NG; g++) {
-        int32_t x = s[g * G];
-#pragma unroll
-        for (int t = 1; t < G; t++)
-            if (g * G + t < N) x *= s[g * G + t];
-        sx ^= (uint32_t)x;
-        mag[g] = (uint32_t)abs(x);
-    }
-    uint32_t P[NG];
-    P[0] = mag[0];
-    ProdChain<1, NG>::run(P, mag);
-    const uint32_t m = (uint32_t)((int32_t)sx >> 31);
-#if EXACT_ACC_PTX
-    AccChain<NL, NG>::add(acc, P, m);
-#else
-    uint32_t cy = m & 1u;
-#pragma unroll
-    for (int l = 0; l < NL; l++) {
-        const uint32_t w = (l < NG ? P[l] : 0u) ^ m;
-        const uint64_t t = (uint64_t)acc[l] + w + cy;
-        acc[l] = (uint32_t)t;
-        cy = (uint32_t)(t >> 32);
-    }
-#endif
 }
 
 // Column form of one term: the sign and the first NG-1 group products give
@@ -244,12 +160,9 @@ __device__ __forceinline__ bool exact_walk(const int32_t *tab, int32_t *s, uint3
                                            volatile const int *abort_flag) {
     using S = ExactShape<N, G>;
     constexpr int NP = S::NP, LOGU = S::LOGU, U = 1 << LOGU;
-    static_assert(FR == 0 || EXACT_COLACC, "float rows need the column form of the term");
     const uint32_t Q = (1u << log_len) >> LOGU;
-#if EXACT_COLACC
     uint64_t col[S::NR > 1 ? S::NR - 1 : 1];
     int64_t colt;
-#endif
     for (uint64_t c = c_begin; c < c_end; c++) {
         if (((c - c_begin) & 255) == 0 && *abort_flag) return false;
         const uint32_t hib = (uint32_t)(c & 1) << log_len;
@@ -286,15 +199,9 @@ __device__ __forceinline__ bool exact_walk(const int32_t *tab, int32_t *s, uint3
                     }
                 }
                 // chunks start at even states, so (-1)^g = (-1)^r
-#if EXACT_COLACC
                 exact_term_col<N, G, FR>(s, col, colt, (uint32_t)(r & 1), r == 0);
-#else
-                exact_term<N, G>(s, acc, (uint32_t)(r & 1));
-#endif
             }
-#if EXACT_COLACC
             FoldCols<S::NR, S::NL>::apply(acc, col, colt);
-#endif
         }
     }
     return true;
@@ -422,11 +329,10 @@ cudaError_t launch_exact_any(int N, int G, const ExactArgs &args, int blocks,
 int occupancy_exact_any(int N, int G);
 bool exact_compiled(int N, int G);
 
-// Largest bound product of the last row group: with column accumulation its
-// magnitude multiplies each word of the running product into a 64-bit
-// column 2^EXACT_LOGU times between folds.
-constexpr uint64_t EXACT_LAST_GROUP_MAX =
-    EXACT_COLACC ? (1ull << (32 - EXACT_LOGU)) : (1ull << 31) - 1;
+// Largest bound product of the last row group: its magnitude multiplies
+// each word of the running product into a 64-bit column 2^EXACT_LOGU times
+// between folds.
+constexpr uint64_t EXACT_LAST_GROUP_MAX = 1ull << (32 - EXACT_LOGU);
 
 // Row order for group size G (rows [g*G, min((g+1)*G, n)) form group g) in
 // which every group's product of row bounds B is < 2^31 and the last

@@ -57,13 +57,17 @@ def build(verbose: bool = False, jobs: int | None = None,
     sources = sorted(CSRC.glob("*.cu"))
     hdr = _newest_header()
     flags = ARCH + NVCC_FLAGS + list(extra_flags or [])
+    # nvcc's intermediate files go to a folder of the build tree
+    tmp = BUILD / "tmp"
+    tmp.mkdir(parents=True, exist_ok=True)
+    env = dict(os.environ, TMPDIR=str(tmp))
 
     def compile_one(src: Path):
         obj = BUILD / (src.stem + ".o")
         if obj.exists() and obj.stat().st_mtime >= max(src.stat().st_mtime, hdr):
             return obj, False, ""
         cmd = [nvcc, *flags, "-c", str(src), "-o", str(obj)]
-        res = subprocess.run(cmd, capture_output=True, text=True)
+        res = subprocess.run(cmd, capture_output=True, text=True, env=env)
         if res.returncode != 0:
             raise RuntimeError(f"nvcc failed for {src.name}:\n{res.stderr}")
         return obj, True, res.stderr
@@ -81,7 +85,7 @@ def build(verbose: bool = False, jobs: int | None = None,
     if rebuilt or not LIB.exists() or any(o.stat().st_mtime > LIB.stat().st_mtime for o in objs):
         tmp = LIB.with_suffix(".so.tmp")
         cmd = [nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart"]
-        res = subprocess.run(cmd, capture_output=True, text=True)
+        res = subprocess.run(cmd, capture_output=True, text=True, env=env)
         if res.returncode != 0:
             raise RuntimeError(f"link failed:\n{res.stderr}")
         os.replace(tmp, LIB)
