@@ -205,6 +205,11 @@ int pg_exact_plan_result(pg_exact_plan *plan, void *stream, uint32_t *out,
 int pg_exact_plan_info(const pg_exact_plan *plan, int *group, int *words,
                        uint64_t *states, uint64_t *imul_per_state,
                        uint64_t *imad_wide_per_state);
+/* Float rows per row group of the plan (0: integer form); with FR > 0 each
+ * group of G rows runs FR - 1 of its G - 1 multiplies on the FP32 pipe and
+ * G - FR as 32-bit IMULs.  Splits pg_exact_plan_info's multiply count by
+ * pipe for the roofline (no reference counterpart). */
+int pg_exact_plan_float_rows(const pg_exact_plan *plan);
 void pg_exact_plan_destroy(pg_exact_plan *plan);
 
 /*
@@ -300,18 +305,24 @@ int pg_glynn_c64(const double *Are, const double *Aim, int batch, int n,
 
 /*
  * pg_exact_permanent for callers that cannot allocate memory (no
- * counterpart in the reference).  Code that runs during CUDA graph capture,
- * plug-ins whose host owns every device allocation, and services that must
- * not grow device memory after start-up cannot call cudaMalloc; this entry
- * point allocates nothing (no device, pinned or host heap memory, no
- * streams).  Its scratch is a fixed 32 KiB __device__ array inside the
- * library, present on every GPU that loads it until exit; orders 2..48 fit
- * and anything larger returns PG_ERANGE.  The caller passes the host matrix
- * and the host output words; `stream` may be NULL (legacy default stream).
+ * counterpart in the reference).  Plug-ins whose host process owns every
+ * device allocation through its own pool, and services that reserve a fixed
+ * device-memory budget at start-up and must not grow it, cannot call
+ * cudaMalloc; this entry point allocates nothing (no device, pinned or host
+ * heap memory, no streams).  Its scratch is a fixed 32 KiB __device__ array
+ * inside the library, present on every GPU that loads it until exit; orders
+ * 2..48 fit, anything larger returns PG_ERANGE, and so does a limb count too
+ * small for the permanent's bound.  It runs the exact kernel's integer-row
+ * form only (slower than pg_exact_permanent at orders 24..32).  The caller
+ * passes the host matrix and the host output words; `stream` may be NULL
+ * (legacy default stream) and is synchronised before the call returns.
  * All calls share the scratch: calls that overlap on the GPU race and must
  * be serialised by the caller.  The first call on each device looks up the
- * scratch address (cudaGetSymbolAddress) and should come before any stream
- * capture.
+ * scratch address (cudaGetSymbolAddress) and keeps it for the process's
+ * life; that first call should come before any stream capture, and calls
+ * after cudaDeviceReset are not supported.  pg_abort() stops it only once
+ * the process's abort word exists (any allocating entry point, pg_abort or
+ * pg_clear_abort creates it; this entry point does not).
  */
 int pg_exact_permanent_noalloc(const int64_t *A, int n, uint32_t *out,
                                int limbs, void *stream);

@@ -163,8 +163,10 @@ __device__ __forceinline__ bool exact_walk(const int32_t *tab, int32_t *s, uint3
     const uint32_t Q = (1u << log_len) >> LOGU;
     uint64_t col[S::NR > 1 ? S::NR - 1 : 1];
     int64_t colt;
+    // the abort word is read every 2^16 states (every chunk for longer ones)
+    const uint64_t poll = log_len >= 16 ? 0 : (1ull << (16 - log_len)) - 1;
     for (uint64_t c = c_begin; c < c_end; c++) {
-        if (((c - c_begin) & 255) == 0 && *abort_flag) return false;
+        if (((c - c_begin) & poll) == 0 && *abort_flag) return false;
         const uint32_t hib = (uint32_t)(c & 1) << log_len;
         for (uint32_t q = 0; q < Q; q++) {
             const uint32_t g32 = (q << LOGU) | hib;
@@ -216,7 +218,24 @@ struct ExactArgs {
     uint64_t chunks;           // chunks to walk: [chunk0, chunk0 + chunks)
     int log_len;               // >= LOGU, <= 30
     uint64_t chunk0;           // first chunk (0 for a whole traversal)
+    int threads = 256;         // threads per block: a multiple of 32, <= 256
 };
+
+// Launch shape for a walk of 2^log_states states: one resident wave of
+// `occ` 256-thread blocks per SM while every thread still gets at least
+// EXACT_MIN_THREAD_STATES states; shorter walks put the same number of
+// whole warps on every SM (smaller blocks) instead of idling SMs.  Chunks
+// are sized for ~128 per thread on long walks and go down to
+// 2^EXACT_MIN_CHUNK_LOG states on short ones (the boundary step is the only
+// one whose column differs between lanes).
+#ifndef EXACT_MIN_THREAD_STATES
+#define EXACT_MIN_THREAD_STATES 64
+#endif
+#ifndef EXACT_MIN_CHUNK_LOG
+#define EXACT_MIN_CHUNK_LOG 2
+#endif
+void exact_launch_shape(int log_states, int occ, int sm_count, uint64_t *blocks,
+                        int *threads, int *log_len);
 
 // Resident blocks per SM requested from ptxas: a register budget of about
 // N + 64 per thread (row sums plus the product/accumulator words) measured
@@ -290,7 +309,7 @@ cudaError_t launch_exact_glynn(const ExactArgs &args, int blocks,
             (int)smem);
         if (e != cudaSuccess) return e;
     }
-    exact_glynn_kernel<N, G, FR><<<blocks, 256, smem, stream>>>(args);
+    exact_glynn_kernel<N, G, FR><<<blocks, args.threads, smem, stream>>>(args);
     return cudaGetLastError();
 }
 

@@ -104,6 +104,40 @@ static void add_i64_at(std::vector<uint32_t> &w, int pos, long long v) {
 }
 
 
+void exact_launch_shape(int log_states, int occ, int sm_count, uint64_t *blocks,
+                        int *threads, int *log_len) {
+    const uint64_t states = 1ull << log_states;
+    const uint64_t sms = (uint64_t)(sm_count < 1 ? 1 : sm_count);
+    const uint64_t cap = (uint64_t)(occ < 1 ? 1 : occ) * sms * 256;
+    uint64_t T = states / EXACT_MIN_THREAD_STATES;
+    if (T > cap) T = cap;
+    uint64_t B;
+    int tpb;
+    if (T / sms < 32) {                       // fewer warps than SMs
+        tpb = 32;
+        B = T / 32 ? T / 32 : 1;
+    } else {                                  // the same whole warps on every SM
+        const uint64_t per_sm = (T / sms) & ~31ull;
+        const uint64_t k = (per_sm + 255) / 256;
+        tpb = (int)((per_sm / k) & ~31ull);
+        B = sms * k;
+    }
+    const uint64_t TT = B * (uint64_t)tpb;
+    int log_T = 0;
+    while ((2ull << log_T) <= TT) log_T++;
+    // ~128 chunks per thread on long walks; short walks take chunks down to
+    // 2^EXACT_MIN_CHUNK_LOG states so that the per-thread ranges stay even
+    int ll = log_states - (log_T + 7);
+    const int want = EXACT_MIN_CHUNK_LOG > EXACT_LOGU ? EXACT_MIN_CHUNK_LOG : EXACT_LOGU;
+    const int min_len = log_states < want ? log_states : want;
+    if (ll < min_len) ll = min_len;
+    if (ll > 30) ll = 30;
+    if (ll < 1) ll = 1;
+    *blocks = B;
+    *threads = tpb;
+    *log_len = ll;
+}
+
 // Everything one exact evaluation needs, built once on the host.
 // Float rows for group size G: within each group the rows are ordered by
 // increasing bound, and the first exact_float_rows(n, G, FR, g) of them must
@@ -152,6 +186,7 @@ struct ExactPlan {
     ChunkPlan chunks{};
     uint64_t chunk0 = 0;
     uint64_t blocks = 0;
+    int threads = 256;
     size_t off_acc = 0, off_status = 0, total = 0;
     std::vector<char> image;     // host image of [tab | init | acc | status]
     // device side (owned by a plan object, or borrowed from a workspace)
@@ -199,20 +234,13 @@ static int plan_build(const int64_t *A, int n, ExactPlan *P) {
         }
     }
     // One resident wave of blocks (occupancy-limited), each thread owning a
-    // contiguous range of ~128 chunks of >= 64 states; small orders use
-    // fewer blocks so every thread still gets >= 512 states.
+    // contiguous range of chunks; short walks shrink the blocks, not the
+    // number of SMs in use (exact_launch_shape).
     const int occ = P->fr ? occupancy_exact_frows(N, G, P->fr) : occupancy_exact_any(N, G);
     const int log_states = n - 1;
-    uint64_t blocks = (uint64_t)occ * dev.sm_count;
-    while (blocks > 1 && ((1ull << log_states) >> 9) < blocks * 256) blocks >>= 1;
-    const uint64_t T = blocks * 256;
-    int log_T = 0;
-    while ((2ull << log_T) <= T) log_T++;
-    int log_len = log_states - (log_T + 7);
-    const int min_len = log_states < 6 ? log_states : 6;
-    if (log_len < min_len) log_len = min_len;
-    if (log_len > 30) log_len = 30;
-    if (log_len < 1) log_len = 1;
+    uint64_t blocks = 0;
+    int log_len = 0;
+    exact_launch_shape(log_states, occ, dev.sm_count, &blocks, &P->threads, &log_len);
     P->chunks.log_len = log_len;
     P->chunks.chunks = 1ull << (log_states - log_len);
     P->blocks = blocks;
@@ -237,6 +265,7 @@ static int plan_launch(ExactPlan *P, cudaStream_t stream) {
     args.chunks = P->chunks.chunks;
     args.log_len = P->chunks.log_len;
     args.chunk0 = P->chunk0;
+    args.threads = P->threads;
     PG_CUDA(cudaMemsetAsync(P->dev + P->off_acc, 0, P->total - P->off_acc, stream));
     PG_CUDA(P->fr ? launch_exact_frows(P->n, P->G, P->fr, args, (int)P->blocks, stream)
                   : launch_exact_any(P->n, P->G, args, (int)P->blocks, stream));
@@ -416,6 +445,10 @@ int pg_exact_plan_info(const pg_exact_plan *plan, int *group, int *words,
     if (imul_per_state) *imul_per_state = (uint64_t)(P.n - P.NG);
     if (imad_wide_per_state) *imad_wide_per_state = (uint64_t)P.NG * (P.NG - 1) / 2;
     return PG_OK;
+}
+
+int pg_exact_plan_float_rows(const pg_exact_plan *plan) {
+    return plan ? plan->p.fr : 0;
 }
 
 void pg_exact_plan_destroy(pg_exact_plan *plan) {

@@ -1,19 +1,22 @@
 // pg_exact_permanent_noalloc: the exact Glynn engine for callers that cannot
 // allocate memory.
 //
-// Some callers cannot call cudaMalloc: code running while a CUDA graph is
-// being captured, plug-ins whose host process owns every device allocation
-// through its own pool, and hard-real-time or memory-budgeted services that
-// must not grow device memory after start-up.  This entry point runs the
-// same kernel as pg_exact_permanent, but its scratch (column tables, initial
-// row sums, the per-word accumulators and the status word) lives in one
-// file-scope __device__ array of fixed size, so the call allocates nothing:
-// no cudaMalloc/cudaFree, no pinned or host heap buffers, no streams.
+// Some callers cannot call cudaMalloc: plug-ins whose host process owns
+// every device allocation through its own pool (a cudaMalloc behind the
+// pool's back breaks its accounting or fails outright), and services that
+// reserve a fixed device-memory budget at start-up and must not grow it
+// afterwards.  This entry point runs the same kernel as pg_exact_permanent
+// (integer rows only, so at orders 24..32 it is somewhat slower than the
+// allocating path, which can keep three rows of each group of four in FP32),
+// but its scratch (column tables, initial row sums, the per-word
+// accumulators and the status word) lives in one file-scope __device__
+// array of fixed size, so the call allocates nothing: no cudaMalloc or
+// cudaFree, no pinned or host heap buffers, no streams.
 //
 // Limits and sharing rules:
-//   * the scratch holds at most PG_NOALLOC_SCRATCH_BYTES (32 KiB); orders
-//     up to 48 (the exact engine's range) fit, larger requests are rejected
-//     with PG_ERANGE before any device work;
+//   * the scratch holds at most PG_NOALLOC_SCRATCH_BYTES (32 KiB); every
+//     order the exact engine takes (2..48) fits, and the byte count of each
+//     request is still checked against the array before any device work;
 //   * every loaded copy of the library keeps this array on every GPU that
 //     loads it, until the process exits;
 //   * all calls share the array and each call leaves its contents behind;
@@ -22,8 +25,16 @@
 //     threads) race on the same words and corrupt each other's result —
 //     serialise them;
 //   * the first call on a device looks up the array's device address with
-//     cudaGetSymbolAddress (once per device, that device current); make that
-//     first call before any stream capture begins.
+//     cudaGetSymbolAddress (once per device, that device current) and keeps
+//     it for the life of the process; make that first call before any
+//     stream capture begins.  Calls after cudaDeviceReset on that device
+//     are not supported (the cached address belongs to the old context);
+//   * the call copies the inputs from and the result to host memory and
+//     synchronises `stream` before it returns;
+//   * pg_abort() reaches this entry point only when the process-wide abort
+//     word already exists (created by pg_abort, pg_clear_abort or any
+//     allocating entry point); this entry point never creates it, and
+//     without it the launch runs to completion.
 #include "pg_internal.h"
 #include "exact_glynn.cuh"
 
@@ -36,7 +47,8 @@
 
 namespace pg {
 
-// Scratch: [tables | init | acc words | status | zero word (abort flag)]
+// Scratch: [tables | init | acc words | status | zero word (abort flag when
+// the process has no abort word yet)]
 static __device__ __align__(256) unsigned char g_noalloc_scratch[PG_NOALLOC_SCRATCH_BYTES];
 
 static std::mutex g_noalloc_mu;
@@ -133,25 +145,22 @@ extern "C" int pg_exact_permanent_noalloc(const int64_t *A, int n, uint32_t *out
     // launch shape as in the allocating path
     const int occ = occupancy_exact_any(n, G);
     const int log_states = n - 1;
-    uint64_t blocks = (uint64_t)occ * dev.sm_count;
-    while (blocks > 1 && ((1ull << log_states) >> 9) < blocks * 256) blocks >>= 1;
-    int log_T = 0;
-    while ((2ull << log_T) <= blocks * 256) log_T++;
-    int log_len = log_states - (log_T + 7);
-    const int min_len = log_states < 6 ? log_states : 6;
-    if (log_len < min_len) log_len = min_len;
-    if (log_len > 30) log_len = 30;
-    if (log_len < 1) log_len = 1;
+    uint64_t blocks = 0;
+    int threads = 256, log_len = 0;
+    exact_launch_shape(log_states, occ, dev.sm_count, &blocks, &threads, &log_len);
 
     ExactArgs args;
     args.tab = (const int32_t *)scratch;
     args.init = (const int32_t *)(scratch + off_init);
     args.acc = (unsigned long long *)(scratch + off_acc);
     args.status = (int *)(scratch + off_status);
-    args.abort_flag = (volatile const int *)(scratch + off_zero);
+    volatile int *abort_word = abort_flag_device_if_created();
+    args.abort_flag = abort_word ? (volatile const int *)abort_word
+                                 : (volatile const int *)(scratch + off_zero);
     args.chunks = 1ull << (log_states - log_len);
     args.log_len = log_len;
     args.chunk0 = 0;
+    args.threads = threads;
     PG_CUDA(launch_exact_any(n, G, args, (int)blocks, s));
 
     long long acc[64];          // NL <= 18 for every compiled shape
@@ -159,7 +168,7 @@ extern "C" int pg_exact_permanent_noalloc(const int64_t *A, int n, uint32_t *out
     PG_CUDA(cudaMemcpyAsync(acc, scratch + off_acc, (size_t)NL * 8, cudaMemcpyDeviceToHost, s));
     PG_CUDA(cudaMemcpyAsync(&status, scratch + off_status, sizeof(int), cudaMemcpyDeviceToHost, s));
     PG_CUDA(cudaStreamSynchronize(s));
-    if (status) return fail(PG_EINTERNAL, "no-alloc launch reported a stop");
+    if (status) return fail(PG_EABORT, "no-alloc exact launch aborted by pg_abort()");
 
     // carry the per-word sums into S (two's complement) and shift by n-1
     uint32_t S[72] = {0};

@@ -46,6 +46,9 @@ int workspace(Workspace **ws, size_t dev_bytes, size_t host_bytes);
 
 // Device pointer of the host-mapped abort word (0 = run, 1 = abort).
 int abort_flag_device(volatile int **dptr);
+// The same pointer when an earlier call already created the word, else
+// nullptr; never allocates.
+volatile int *abort_flag_device_if_created();
 
 // ---- chunk plan -----------------------------------------------------------
 // A traversal of 2^s Gray states is cut into 2^(s-log_len) aligned chunks of

@@ -119,6 +119,11 @@ int abort_flag_device(volatile int **dptr) {
     return PG_OK;
 }
 
+volatile int *abort_flag_device_if_created() {
+    std::lock_guard<std::mutex> lock(g_abort_mu);
+    return g_abort_dev;
+}
+
 ChunkPlan plan_chunks(int log_states, int min_log_len, uint64_t target_chunks) {
     // Largest chunk count that is a power of two <= target, keeping chunks at
     // least 2^min_log_len long and at most 2^30 (accumulator headroom), and

@@ -108,6 +108,22 @@ def test_binary_cases_exact(lib):
         assert permgpu.binary_permanent(c["matrix"]) == int(c["permanent"])
 
 
+def test_binary40_workload_at_full_size(lib):
+    # The eight 40 x 40 Bernoulli(0.5) benchmark matrices (seeds 300..307)
+    # through the whole binary API (matching blocks, exact engine) against
+    # per(A) modulo two primes from pg_binary_residues: an independent
+    # traversal whose residues are pinned to the reference's
+    # binary_permanent_mod_p (perm_binary.py:943-1005, perm_binary_omp.c:
+    # 236-347).  Each matrix is a full 2^39-state walk on both sides.
+    import permgpu
+    from permgpu import workloads
+    primes = [2_147_483_647, 2_147_483_629]
+    for m in workloads.binary40(8):
+        v = permgpu.binary_permanent(m.tolist())
+        assert v > 0
+        assert lib.binary_residues(m, primes) == [v % p for p in primes]
+
+
 def test_binary_residue_path_equals_exact_path(lib):
     import permgpu
     from permgpu.crt import binary_block_bound, binary_primes_above

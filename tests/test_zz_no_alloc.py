@@ -1,23 +1,29 @@
 """GPU test of pg_exact_permanent_noalloc, the entry point for callers that
-cannot allocate memory (code running under CUDA graph capture, plug-ins
-whose host owns all device allocations, services with a fixed memory
-budget).  It must give exactly what the allocating entry point
-pg_exact_permanent gives — integers, so the tolerance is zero — on two
-calls in a row (the shared scratch keeps the previous call's contents and
-must be re-zeroed), and reject problems beyond its 32 KiB scratch.
+cannot allocate device memory: plug-ins whose host process owns every device
+allocation through its own pool, and services that reserve a fixed memory
+budget at start-up and must not grow it.  The entry point keeps its scratch
+in a fixed 32 KiB array inside the library instead of calling cudaMalloc.
+
+It must give exactly what the allocating entry point pg_exact_permanent
+gives — integers, so the tolerance is zero — on two calls in a row (the
+shared scratch keeps the previous call's contents and must be re-zeroed),
+on the legacy default stream and on a stream the caller created, and it
+must reject orders above 48 and output buffers too small for the bound.
 
 Collected last (file name) so a failure here never hides the other tests;
 it passes alone in a fresh process as well as after them.
 """
 
 import ctypes
+import threading
+import time
 
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
 
-PG_OK, PG_ERANGE, PG_EOVERFLOW = 0, 2, 7
+PG_OK, PG_ERANGE, PG_EABORT, PG_EOVERFLOW = 0, 2, 5, 7
 
 
 def _call(fn, a, limbs, *extra):
@@ -62,6 +68,21 @@ def test_noalloc_alternating_matrices_do_not_leak_state():
             assert lib.limbs_to_int(got) == w
 
 
+def test_noalloc_on_a_caller_created_stream():
+    import torch
+    lib, h = _lib()
+    rng = np.random.default_rng(11)
+    a = rng.integers(-8, 9, (26, 26), dtype=np.int64)
+    limbs = lib.exact_limbs(a)
+    st, want = _call(h.pg_exact_permanent, a, limbs)
+    assert st == PG_OK, h.pg_last_error()
+    stream = torch.cuda.Stream()
+    for _ in range(2):
+        st, got = _call(h.pg_exact_permanent_noalloc, a, limbs, ctypes.c_void_p(stream.cuda_stream))
+        assert st == PG_OK, h.pg_last_error()
+        assert got.tolist() == want.tolist()
+
+
 def test_noalloc_rejects_beyond_its_limits():
     lib, h = _lib()
     st, _ = _call(h.pg_exact_permanent_noalloc, np.ones((49, 49), np.int64), 16, None)
@@ -69,3 +90,32 @@ def test_noalloc_rejects_beyond_its_limits():
     assert b"2 <= n <= 48" in h.pg_last_error()
     st, _ = _call(h.pg_exact_permanent_noalloc, np.full((5, 5), 1 << 40, np.int64), 16, None)
     assert st == PG_EOVERFLOW
+    # 12 x 12 entries in [-8, 8]: the bound needs more than one 32-bit limb
+    a = np.random.default_rng(3).integers(-8, 9, (12, 12), dtype=np.int64)
+    st, _ = _call(h.pg_exact_permanent_noalloc, a, 1, None)
+    assert st == PG_ERANGE
+    assert b"limb count" in h.pg_last_error()
+
+
+def test_noalloc_stops_on_pg_abort_once_the_abort_word_exists():
+    # pg_clear_abort creates the process's abort word (an allocation made
+    # here by the test, not by the entry point); a 40 x 40 0/1 walk takes
+    # seconds, and pg_abort from another host thread ends it early
+    lib, h = _lib()
+    h.pg_clear_abort()
+    a = (np.random.default_rng(300).random((40, 40)) < 0.5).astype(np.int64)
+    timer = threading.Timer(0.2, h.pg_abort)
+    t0 = time.perf_counter()
+    timer.start()
+    try:
+        st, _ = _call(h.pg_exact_permanent_noalloc, a, lib.exact_limbs(a), None)
+    finally:
+        timer.join()
+        h.pg_clear_abort()
+    assert st == PG_EABORT, h.pg_last_error()
+    assert time.perf_counter() - t0 < 1.5
+    # re-armed: the next call completes and agrees with the allocating path
+    b = np.random.default_rng(5).integers(-8, 9, (18, 18), dtype=np.int64)
+    st, got = _call(h.pg_exact_permanent_noalloc, b, lib.exact_limbs(b), None)
+    assert st == PG_OK
+    assert lib.limbs_to_int(got) == lib.exact_permanent(b, lib.exact_limbs(b))
