@@ -474,6 +474,23 @@ def run_gpu_batch(args, world, rank, local):
     plan.close()
 
 
+def exact_dyadic(matrix):
+    """(per(A) as a Fraction, row exponents k, exact integer-row matrix):
+    every FP64 entry is a dyadic rational, so row i times 2^k_i is an
+    integer row and per(A) = per(A_int) / 2^(sum k_i); per(A_int) comes from
+    the exact integer path (permgpu.matrix_permanent, residue engine for
+    entries beyond the exact engine's widths)."""
+    from fractions import Fraction
+    import permgpu
+    rows, ks = [], []
+    for row in matrix:
+        fr = [Fraction(float(v)) for v in row]
+        k = max(max(f.denominator.bit_length() - 1 for f in fr), 0)
+        rows.append([int(f * (1 << k)) for f in fr])
+        ks.append(k)
+    return Fraction(permgpu.matrix_permanent(rows), 1 << sum(ks)), ks, rows
+
+
 def run_gpu_float28(args, world, rank, local):
     """float28: 256 float64 matrices 28x28, entries N(0, 1/28), seed 5 (+rank);
     one step = forward + hand-written gradient of the whole batch;
@@ -502,6 +519,41 @@ def run_gpu_float28(args, world, rank, local):
         want, _ = oracle.glynn_f64(A_host[b], os.cpu_count() or 1)
         rel.append(abs(per[b].item() - want) / s[b].item())
     g = grad.cpu().numpy()
+    # against the EXACT value of the same FP64 inputs (dyadic rationals made
+    # integer row by row, exact integer permanents): the forward of sampled
+    # matrices and 8 sampled gradient entries of each (the minors, exact),
+    # errors relative to the sums of |terms| the kernel returns
+    from fractions import Fraction
+    import permgpu
+    exact_fwd, exact_grad = [], []
+    sample = [0, batch - 1] if rank == 0 else []
+    pick = np.random.default_rng(28)
+    for b in sample:
+        want, ks, rows = exact_dyadic(A_host[b])
+        exact_fwd.append(abs(Fraction(per[b].item()) - want) / Fraction(s[b].item()))
+        for _ in range(8):
+            i, j = (int(x) for x in pick.integers(0, n, 2))
+            minor = [r[:j] + r[j + 1:] for t, r in enumerate(rows) if t != i]
+            gw = Fraction(permgpu.matrix_permanent(minor), 1 << (sum(ks) - ks[i]))
+            exact_grad.append(abs(Fraction(float(g[b, i, j])) - gw) /
+                              Fraction(gs[b, i].item()))
+    # forward-only arm (the same traversal without the gradient columns)
+    for _ in range(2):
+        permanent_f64(A, want_grad=False)
+    torch.cuda.synchronize()
+    ms_fwd = []
+    for _ in range(max(1, args.steps // 2)):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        permanent_f64(A, want_grad=False)
+        e1.record(stream)
+        e1.synchronize()
+        ms_fwd.append(e0.elapsed_time(e1))
+    from permgpu import _lib
+    fma32 = _lib.probe_int_throughput(5)        # fma.rn.f32 thread-instructions/s
+    fma64 = _lib.probe_int_throughput(6)
     exp_err = max(float(np.max(np.abs((A_host[b] * g[b]).sum(axis=1) - per[b].item())
                                / (np.abs(A_host[b]) * gs[b].cpu().numpy()[:, None]).sum(axis=1)))
                   for b in range(batch))
@@ -532,6 +584,18 @@ def run_gpu_float28(args, world, rank, local):
     clk = clocks.stop()
     step_ms = max_over_ranks(world, statistics.mean(ms))
     e2e_s = max_over_ranks(world, statistics.mean(e2e))
+    fwd_ms = statistics.mean(ms_fwd)
+    # roofline: FP32-pipe instructions of the algorithm per state, counted
+    # from the kernel source for the n live rows (lanes): one double-float
+    # add per row update (11 FP32 instructions), 10 double-float products in
+    # the 5-level butterfly (7 each), one add for the forward term and 1 + M
+    # (M = 4) for the gradient columns; the forward-only walk drops the
+    # gradient's 5 products (E) and 5 adds
+    df_add, df_mul = 11, 7
+    fwd_bwd_ops = n * (df_add * (1 + 1 + 1 + 4) + df_mul * 10)
+    fwd_ops = n * (df_add * 2 + df_mul * 5)
+    achieved = states * fwd_bwd_ops / (step_ms * 1e-3)
+    achieved_fwd = states * fwd_ops / (fwd_ms * 1e-3)
     if rank == 0:
         print(json.dumps({
             "metric": "FP64 Glynn forward+gradient steps/s (256 x 28x28)",
@@ -545,7 +609,21 @@ def run_gpu_float28(args, world, rank, local):
                        "l2": "flushed between timed steps (256 MiB write)"},
             "max_rel_err_forward_vs_oracle": max(rel),
             "max_rel_err_row_expansion": exp_err,
+            "max_rel_err_forward_vs_exact": float(max(exact_fwd)),
+            "max_rel_err_gradient_vs_exact": float(max(exact_grad)),
+            "exact_check": f"matrices {sample} of the batch: forward and 8 gradient entries each "
+                           "against exact integer permanents of the row-scaled dyadic inputs; "
+                           "errors relative to the kernel's sums of |terms|",
             "tolerance": 1e-10,
+            "forward_only_ms": fwd_ms,
+            "gradient_cost_ratio": step_ms / fwd_ms,
+            "roofline": {"bound": "fp32 issue", "achieved": achieved / 1e12, "peak": fma32 / 1e12,
+                         "unit": "Tops/s", "frac": achieved / fma32, "traffic": None,
+                         "peak_source": "measured live: pg_probe_int_throughput fma.rn.f32",
+                         "work_per_state": {"fp32_instructions": fwd_bwd_ops,
+                                            "forward_only": fwd_ops},
+                         "frac_forward_only": achieved_fwd / fma32,
+                         "fp64_fma_ops_per_s": fma64},
             "e2e": {"value": world * states / e2e_s, "unit": "steps/s",
                     "h2d_bytes_per_step": int(A_host.nbytes),
                     "d2h_bytes_per_step": int(batch * 8 + A_host.nbytes),

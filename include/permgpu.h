@@ -119,7 +119,7 @@ int pg_necklace_orbit_stats(int n, uint64_t *representatives, uint64_t *words);
 /*
  * Affine-polynomial residues: out[t*(n+1) + d] = coefficient of x^d in
  * per(C + x L) mod moduli[t], for row-major n x n signed 64-bit C and L,
- * 0 <= n <= 32 and odd moduli 3 <= m < 2^30 (they need not be prime).  All
+ * 0 <= n <= 63 and odd moduli 3 <= m < 2^30 (they need not be prime).  All
  * moduli run in one launch.  Replaces perm_polynomial_ext.affine_permanent_mod
  * (perm_polynomial_omp.c:1207-1360, engine :434-486, :612-779); the
  * principal-permanent polynomial per(I + x A) and the rook polynomials
@@ -128,6 +128,20 @@ int pg_necklace_orbit_stats(int n, uint64_t *representatives, uint64_t *words);
  */
 int pg_affine_residues(const int64_t *C, const int64_t *L, int n,
                        const uint64_t *moduli, int k, uint64_t *out);
+
+/*
+ * pg_affine_residues restricted to the Gray states [state_lo, state_hi) of
+ * the walk (2 <= n <= 63): out[t*(n+1) + d] = coefficient of x^d of the
+ * unscaled Glynn sum over those states, sum_g (-1)^g prod_i (c_i(g) +
+ * x l_i(g)) mod moduli[t] (NOT multiplied by 2^(1-n)).  Windows of a
+ * partition of [0, 2^(n-1)) add up to 2^(n-1) per(C + x L); they split one
+ * polynomial across devices the way the reference's native engine splits
+ * the walk across threads (perm_polynomial_omp.c:612-636).  The window
+ * interface has no reference counterpart.
+ */
+int pg_affine_residues_partial(const int64_t *C, const int64_t *L, int n,
+                               uint64_t state_lo, uint64_t state_hi,
+                               const uint64_t *moduli, int k, uint64_t *out);
 
 /*
  * Permanent modulo 3 (*out in {0, 1, 2}) by Ryser's formula over F_3 with
@@ -263,9 +277,11 @@ int pg_batch_exact(const int64_t *A, const int64_t *offsets,
  *   abs_sum[b]      = 2^(1-n) sum |terms|  (error scale of per[b])
  *   grad_abs[b][i]  = 2^(1-n) sum |prod_{l != i} s_l|  (scale of row i)
  * grad / abs_sum / grad_abs may be NULL (grad NULL: forward only).
- * 2 <= n <= 32.  Replaces permanent_parallel_real (perm_parallel_cuda.cu:
- * 343-414, forward only, one matrix); the gradient has no reference
- * counterpart.  Synchronises `stream` before returning.
+ * 2 <= n <= 63; the gradient for n <= 32 (orders 33..63 run forward only,
+ * two rows per lane, and return PG_ERANGE when grad or grad_abs is given).
+ * Replaces permanent_parallel_real (perm_parallel_cuda.cu:343-414, forward
+ * only, one matrix, n <= 63); the gradient has no reference counterpart.
+ * Synchronises `stream` before returning.
  */
 int pg_glynn_f64_dev(const double *A, int batch, int n, double *per,
                      double *grad, double *abs_sum, double *grad_abs,
@@ -274,7 +290,7 @@ int pg_glynn_f64_dev(const double *A, int batch, int n, double *per,
 /*
  * pg_glynn_f64_dev with host pointers: A [batch][n][n] f64 in, per[batch],
  * grad [batch][n][n] (NULL: forward only) and abs_sum[batch] (nullable)
- * out; 0 <= n <= 32.  Device buffers for the call are allocated and freed
+ * out; 0 <= n <= 63 (gradient: n <= 32).  Device buffers for the call are allocated and freed
  * inside, so plain ctypes callers need no device memory of their own.
  * Replaces permanent_parallel_real (perm_parallel_cuda.cu:343-414) for a
  * whole batch, with the gradient.
@@ -286,7 +302,7 @@ int pg_glynn_f64_fwd_bwd(const double *A, int batch, int n, double *per,
  * Complex FP64 Glynn permanent (forward) for a batch of complex matrices
  * given as separate real and imaginary planes (device pointers, [batch][n]
  * [n] each); per_re/per_im receive per(A_b), abs_sum (nullable) the error
- * scale 2^(1-n) sum |terms|.  2 <= n <= 32.  Replaces
+ * scale 2^(1-n) sum |terms|.  2 <= n <= 63.  Replaces
  * permanent_parallel_complex (perm_parallel_cuda.cu:416-498).
  */
 int pg_glynn_c64_dev(const double *Are, const double *Aim, int batch, int n,
@@ -296,12 +312,27 @@ int pg_glynn_c64_dev(const double *Are, const double *Aim, int batch, int n,
 /*
  * pg_glynn_c64_dev with host pointers: real and imaginary planes
  * [batch][n][n] in, per_re/per_im[batch] and abs_sum[batch] (nullable) out;
- * 0 <= n <= 32.  Device buffers for the call are allocated and freed
+ * 0 <= n <= 63.  Device buffers for the call are allocated and freed
  * inside.  Replaces permanent_parallel_complex (perm_parallel_cuda.cu:
  * 416-498) for a whole batch.
  */
 int pg_glynn_c64(const double *Are, const double *Aim, int batch, int n,
                  double *per_re, double *per_im, double *abs_sum);
+
+/*
+ * FP64 Glynn sum over a Gray window of one real (Aim NULL) or complex
+ * matrix, host pointers: sum_re/sum_im = sum over states g in [lo, hi) of
+ * (-1)^g prod_i s_i(g), with s_i(g) = sum_j d_j(g) a_ij and the last
+ * column's sign fixed, NOT divided by 2^(n-1); abs_sum (nullable) = the sum
+ * of |terms| over the window (its error scale).  2 <= n <= 63,
+ * lo <= hi <= 2^(n-1).  Windows split one FP64 permanent across devices
+ * (per(A) = 2^(1-n) times the sum of the window sums) the way rivin-perm's
+ * permanent_glynn_kernel splits the walk across threads
+ * (perm_parallel_cuda.cu:68-209); the window interface itself has no
+ * reference counterpart.
+ */
+int pg_glynn_window(const double *Are, const double *Aim, int n, uint64_t lo,
+                    uint64_t hi, double *sum_re, double *sum_im, double *abs_sum);
 
 /*
  * pg_exact_permanent for callers that cannot allocate memory (no
@@ -328,10 +359,11 @@ int pg_exact_permanent_noalloc(const int64_t *A, int n, uint32_t *out,
                                int limbs, void *stream);
 
 /*
- * Integer-pipe throughput probe (roofline denominator; no reference
- * counterpart): variant 0 mad.lo.u32, 1 mad.wide.u32 (64-bit addend),
- * 2 mad.hi.u32, 3 add.u32, 4 mul.wide.u32 (no addend); writes
- * thread-instructions per second for the whole GPU.
+ * Pipe throughput probe (roofline denominator; a measurement utility with
+ * no reference counterpart): variant 0 mad.lo.u32, 1 mad.wide.u32 (64-bit
+ * addend), 2 mad.hi.u32, 3 add.u32, 4 mul.wide.u32 (no addend), 5
+ * fma.rn.f32, 6 fma.rn.f64; writes thread-instructions per second for the
+ * whole GPU.
  */
 int pg_probe_int_throughput(int variant, int iters, double *ops_per_second);
 

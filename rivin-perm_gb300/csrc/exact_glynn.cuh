@@ -214,6 +214,12 @@ struct ExactArgs {
     const int32_t *init;       // [NP] row sums of the all-plus state
     unsigned long long *acc;   // [NL] per-word sums (two's complement, zeroed)
     int *status;
+    // Launch ticket and result words: the last block to finish copies acc
+    // and the status into out[0..NL] and re-zeroes acc, status and ticket,
+    // so back-to-back launches of one plan need no memset (zero all four
+    // once before the first launch).
+    unsigned int *ticket;
+    unsigned long long *out;   // [NL + 1]: the words, then the status
     volatile const int *abort_flag;
     uint64_t chunks;           // chunks to walk: [chunk0, chunk0 + chunks)
     int log_len;               // >= LOGU, <= 30
@@ -296,6 +302,20 @@ exact_glynn_kernel(ExactArgs a) {
         atomicAdd(a.acc + threadIdx.x, (unsigned long long)t);
     }
     if (threadIdx.x == 0 && any_abort) atomicExch(a.status, 1);
+    // the block that finishes last moves the totals out and re-arms the
+    // accumulators (the fence orders this block's atomics before its ticket)
+    __threadfence();
+    __syncthreads();
+    __shared__ bool last;
+    if (threadIdx.x == 0) last = atomicAdd(a.ticket, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (last) {
+        if (threadIdx.x < NL) a.out[threadIdx.x] = atomicExch(a.acc + threadIdx.x, 0ull);
+        if (threadIdx.x == 0) {
+            a.out[NL] = (unsigned long long)(unsigned)atomicExch(a.status, 0);
+            atomicExch(a.ticket, 0u);
+        }
+    }
 }
 
 template <int N, int G, int FR = 0>

@@ -125,11 +125,16 @@ void exact_launch_shape(int log_states, int occ, int sm_count, uint64_t *blocks,
     const uint64_t TT = B * (uint64_t)tpb;
     int log_T = 0;
     while ((2ull << log_T) <= TT) log_T++;
-    // ~128 chunks per thread on long walks; short walks take chunks down to
-    // 2^EXACT_MIN_CHUNK_LOG states so that the per-thread ranges stay even
+    // ~128 chunks per thread on long walks; shorter walks keep chunks of 64
+    // states while every thread still gets >= 6 of them, and below that go
+    // down to 2^EXACT_MIN_CHUNK_LOG states so the per-thread ranges stay
+    // even (the chunk's first step is the only divergent one)
     int ll = log_states - (log_T + 7);
+    int fit = 0;
+    while (fit < 6 && (states >> (fit + 1)) / TT >= 6) fit++;
     const int want = EXACT_MIN_CHUNK_LOG > EXACT_LOGU ? EXACT_MIN_CHUNK_LOG : EXACT_LOGU;
-    const int min_len = log_states < want ? log_states : want;
+    const int floor_len = fit > want ? fit : want;
+    const int min_len = log_states < floor_len ? log_states : floor_len;
     if (ll < min_len) ll = min_len;
     if (ll > 30) ll = 30;
     if (ll < 1) ll = 1;
@@ -187,7 +192,7 @@ struct ExactPlan {
     uint64_t chunk0 = 0;
     uint64_t blocks = 0;
     int threads = 256;
-    size_t off_acc = 0, off_status = 0, total = 0;
+    size_t off_acc = 0, off_status = 0, off_out = 0, total = 0;
     std::vector<char> image;     // host image of [tab | init | acc | status]
     // device side (owned by a plan object, or borrowed from a workspace)
     char *dev = nullptr;
@@ -216,8 +221,9 @@ static int plan_build(const int64_t *A, int n, ExactPlan *P) {
     P->need_bits = bound_bits(A, n) + 2;
     const size_t off_init = align_up((size_t)NCOL * 2 * NP * 4, 256);
     P->off_acc = align_up(off_init + (size_t)NP * 4, 256);
-    P->off_status = align_up(P->off_acc + (size_t)P->NL * 8, 256);
-    P->total = align_up(P->off_status + 16, 256);
+    P->off_status = align_up(P->off_acc + (size_t)P->NL * 8, 256);   // status, ticket at +8
+    P->off_out = align_up(P->off_status + 16, 256);
+    P->total = align_up(P->off_out + (size_t)(P->NL + 1) * 8, 256);
     P->image.assign(P->total, 0);
     int32_t *tab = (int32_t *)P->image.data();
     int32_t *init = (int32_t *)(P->image.data() + off_init);
@@ -247,14 +253,17 @@ static int plan_build(const int64_t *A, int n, ExactPlan *P) {
     return PG_OK;
 }
 
-// Upload tables (async on P->stream).
+// Upload tables and zero the accumulators, status, ticket and result words
+// (async on P->stream).  Launches re-zero what they use, so this runs once
+// per plan.
 static int plan_upload(ExactPlan *P) {
     std::memcpy(P->host, P->image.data(), P->total);
     PG_CUDA(cudaMemcpyAsync(P->dev, P->host, P->off_acc, cudaMemcpyHostToDevice, P->stream));
+    PG_CUDA(cudaMemsetAsync(P->dev + P->off_acc, 0, P->total - P->off_acc, P->stream));
     return PG_OK;
 }
 
-// Zero the accumulators and launch (async on `stream`).
+// One launch (async on `stream`): a single kernel, no memset.
 static int plan_launch(ExactPlan *P, cudaStream_t stream) {
     ExactArgs args;
     args.tab = (const int32_t *)P->dev;
@@ -266,7 +275,8 @@ static int plan_launch(ExactPlan *P, cudaStream_t stream) {
     args.log_len = P->chunks.log_len;
     args.chunk0 = P->chunk0;
     args.threads = P->threads;
-    PG_CUDA(cudaMemsetAsync(P->dev + P->off_acc, 0, P->total - P->off_acc, stream));
+    args.ticket = (unsigned int *)(P->dev + P->off_status + 8);
+    args.out = (unsigned long long *)(P->dev + P->off_out);
     PG_CUDA(P->fr ? launch_exact_frows(P->n, P->G, P->fr, args, (int)P->blocks, stream)
                   : launch_exact_any(P->n, P->G, args, (int)P->blocks, stream));
     return PG_OK;
@@ -292,14 +302,13 @@ static int plan_restrict(ExactPlan *P, uint64_t lo, uint64_t hi) {
 static int plan_finish(ExactPlan *P, cudaStream_t stream, uint32_t *out, int limbs) {
     if (32 * limbs < P->need_bits)
         return fail(PG_ERANGE, "output limb count too small for the permanent bound");
-    PG_CUDA(cudaMemcpyAsync(P->host + P->off_acc, P->dev + P->off_acc,
-                            P->total - P->off_acc, cudaMemcpyDeviceToHost, stream));
-    PG_CUDA(cudaStreamSynchronize(stream));
-    if (*(int *)(P->host + P->off_status))
-        return fail(PG_EABORT, "exact launch aborted by pg_abort()");
     const int NL = P->NL, W = NL + 3;
+    PG_CUDA(cudaMemcpyAsync(P->host + P->off_out, P->dev + P->off_out, (size_t)(NL + 1) * 8,
+                            cudaMemcpyDeviceToHost, stream));
+    PG_CUDA(cudaStreamSynchronize(stream));
+    const long long *acc = (const long long *)(P->host + P->off_out);
+    if (acc[NL]) return fail(PG_EABORT, "exact launch aborted by pg_abort()");
     std::vector<uint32_t> S(W, 0);
-    const long long *acc = (const long long *)(P->host + P->off_acc);
     for (int l = 0; l < NL; l++) add_i64_at(S, l, acc[l]);
     const int sh = P->n - 1;
     for (int b = 0; b < sh; b++)
@@ -382,11 +391,12 @@ int pg_exact_partial(const int64_t *A, int n, uint64_t state_lo, uint64_t state_
     P.stream = ws->stream;
     if ((st = plan_upload(&P)) != PG_OK) return st;
     if ((st = plan_launch(&P, P.stream)) != PG_OK) return st;
-    PG_CUDA(cudaMemcpyAsync(P.host + P.off_acc, P.dev + P.off_acc, P.total - P.off_acc,
+    PG_CUDA(cudaMemcpyAsync(P.host + P.off_out, P.dev + P.off_out, (size_t)(P.NL + 1) * 8,
                             cudaMemcpyDeviceToHost, P.stream));
     PG_CUDA(cudaStreamSynchronize(P.stream));
-    if (*(int *)(P.host + P.off_status)) return fail(PG_EABORT, "aborted by pg_abort()");
-    std::memcpy(words, P.host + P.off_acc, (size_t)P.NL * 8);
+    if (((const long long *)(P.host + P.off_out))[P.NL])
+        return fail(PG_EABORT, "aborted by pg_abort()");
+    std::memcpy(words, P.host + P.off_out, (size_t)P.NL * 8);
     *nwords = P.NL;
     return PG_OK;
 }

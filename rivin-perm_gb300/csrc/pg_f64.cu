@@ -25,53 +25,14 @@
 // kernel reduces the slots of each matrix (deterministic order).  The sum of
 // |terms| is accumulated alongside, so every result carries its error scale.
 #include "pg_internal.h"
+#include "df_arith.cuh"
+#include "f64_wide.cuh"
 
 #include <cmath>
 #include <cstring>
 #include <vector>
 
 namespace pg {
-
-struct df { float hi, lo; };
-
-__device__ __forceinline__ df df_from(double x) {
-    df r;
-    r.hi = (float)x;
-    r.lo = (float)(x - (double)r.hi);
-    return r;
-}
-__device__ __forceinline__ double df_to(df a) { return (double)a.hi + (double)a.lo; }
-
-__device__ __forceinline__ df df_add(df a, df b) {
-    const float s = a.hi + b.hi;
-    const float bb = s - a.hi;
-    float e = (a.hi - (s - bb)) + (b.hi - bb);
-    e += a.lo + b.lo;
-    df r;
-    r.hi = s + e;
-    r.lo = e - (r.hi - s);
-    return r;
-}
-__device__ __forceinline__ df df_neg(df a) { return df{-a.hi, -a.lo}; }
-__device__ __forceinline__ df df_mul(df a, df b) {
-    const float p = a.hi * b.hi;
-    float e = fmaf(a.hi, b.hi, -p);
-    e = fmaf(a.hi, b.lo, e);
-    e = fmaf(a.lo, b.hi, e);
-    df r;
-    r.hi = p + e;
-    r.lo = e - (r.hi - p);
-    return r;
-}
-__device__ __forceinline__ df df_shfl_xor(df a, int off) {
-    return df{__shfl_xor_sync(0xffffffffu, a.hi, off), __shfl_xor_sync(0xffffffffu, a.lo, off)};
-}
-__device__ __forceinline__ void kahan(double &sum, double &comp, double x) {
-    const double y = x - comp;
-    const double t = sum + y;
-    comp = (t - sum) - y;
-    sum = t;
-}
 
 // Per-warp scratch slot layout (doubles).
 __host__ __device__ constexpr int f64_slot_doubles(int n) { return 4 + 2 * n * n + n; }
@@ -306,10 +267,17 @@ static cudaError_t launch_f64_any(int n, const F64Args &a, cudaStream_t s) {
 extern "C" int pg_glynn_f64_dev(const double *A, int batch, int n, double *per, double *grad,
                                 double *abs_sum, double *grad_abs, void *stream) {
     using namespace pg;
-    if (batch < 0 || n < 0 || n > 32) return fail(PG_ERANGE, "FP64 engine supports 0 <= n <= 32");
+    if (batch < 0 || n < 0 || n > 63) return fail(PG_ERANGE, "FP64 engine supports 0 <= n <= 63");
     if (batch == 0) return PG_OK;
     if (!A || !per) return fail(PG_EINVAL, "null argument");
     if (n <= 1) return fail(PG_ERANGE, "orders 0 and 1 are handled by the caller");
+    if (n > 32) {
+        // orders 33..63: forward only, two rows per lane (f64_wide.cuh)
+        if (grad || grad_abs)
+            return fail(PG_ERANGE, "the FP64 gradient supports n <= 32 (forward up to 63)");
+        return glynn_wide_run(A, nullptr, batch, n, 0, 1ull << (n - 1), true, per, nullptr,
+                              abs_sum, (cudaStream_t)stream);
+    }
     DeviceInfo dev;
     int st = device_info(&dev);
     if (st != PG_OK) return st;
@@ -373,15 +341,6 @@ extern "C" int pg_glynn_f64_dev(const double *A, int batch, int n, double *per, 
 // flushes into per-warp slots); complex counterpart of rivin-perm
 // permanent_glynn_kernel<true> (perm_parallel_cuda.cu:68-209).
 namespace pg {
-
-struct dc { df re, im; };
-
-__device__ __forceinline__ dc dc_mul(dc a, dc b) {
-    dc r;
-    r.re = df_add(df_mul(a.re, b.re), df_neg(df_mul(a.im, b.im)));
-    r.im = df_add(df_mul(a.re, b.im), df_mul(a.im, b.re));
-    return r;
-}
 
 struct C64Args {
     const double *Are, *Aim;   // [batch][n][n]
@@ -517,9 +476,12 @@ static cudaError_t launch_c64_any(int n, const C64Args &a, cudaStream_t s) {
 extern "C" int pg_glynn_c64_dev(const double *Are, const double *Aim, int batch, int n,
                                 double *per_re, double *per_im, double *abs_sum, void *stream) {
     using namespace pg;
-    if (batch < 0 || n < 2 || n > 32) return fail(PG_ERANGE, "complex FP64 engine supports 2 <= n <= 32");
+    if (batch < 0 || n < 2 || n > 63) return fail(PG_ERANGE, "complex FP64 engine supports 2 <= n <= 63");
     if (batch == 0) return PG_OK;
     if (!Are || !Aim || !per_re || !per_im) return fail(PG_EINVAL, "null argument");
+    if (n > 32)   // two rows per lane (f64_wide.cuh)
+        return glynn_wide_run(Are, Aim, batch, n, 0, 1ull << (n - 1), true, per_re, per_im,
+                              abs_sum, (cudaStream_t)stream);
     DeviceInfo dev;
     int st = device_info(&dev);
     if (st != PG_OK) return st;
@@ -561,9 +523,11 @@ extern "C" int pg_glynn_c64_dev(const double *Are, const double *Aim, int batch,
 extern "C" int pg_glynn_f64_fwd_bwd(const double *A, int batch, int n, double *per,
                                     double *grad, double *abs_sum) {
     using namespace pg;
-    if (batch < 0 || n < 0 || n > 32) return fail(PG_ERANGE, "FP64 engine supports 0 <= n <= 32");
+    if (batch < 0 || n < 0 || n > 63) return fail(PG_ERANGE, "FP64 engine supports 0 <= n <= 63");
     if (batch == 0) return PG_OK;
     if (!per || (n > 0 && !A)) return fail(PG_EINVAL, "null argument");
+    if (n > 32 && grad)
+        return fail(PG_ERANGE, "the FP64 gradient supports n <= 32 (forward up to 63)");
     if (n <= 1) {
         for (int b = 0; b < batch; b++) {
             per[b] = n == 0 ? 1.0 : A[b];
@@ -601,14 +565,14 @@ extern "C" int pg_glynn_f64_fwd_bwd(const double *A, int batch, int n, double *p
 
 // pg_glynn_c64_dev with host pointers: the real and imaginary planes
 // [batch][n][n] in, per_re/per_im[batch] and abs_sum[batch] (nullable)
-// out; 0 <= n <= 32 (n <= 1 on the host).  Device buffers for the call are
+// out; 0 <= n <= 63 (n <= 1 on the host).  Device buffers for the call are
 // allocated and freed inside.  Replaces permanent_parallel_complex
 // (perm_parallel_cuda.cu:416-498), host planes in and host values out.
 extern "C" int pg_glynn_c64(const double *Are, const double *Aim, int batch, int n,
                             double *per_re, double *per_im, double *abs_sum) {
     using namespace pg;
-    if (batch < 0 || n < 0 || n > 32)
-        return fail(PG_ERANGE, "complex FP64 engine supports 0 <= n <= 32");
+    if (batch < 0 || n < 0 || n > 63)
+        return fail(PG_ERANGE, "complex FP64 engine supports 0 <= n <= 63");
     if (batch == 0) return PG_OK;
     if (!per_re || !per_im || (n > 0 && (!Are || !Aim))) return fail(PG_EINVAL, "null argument");
     if (n <= 1) {

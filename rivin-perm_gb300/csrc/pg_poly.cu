@@ -301,10 +301,12 @@ static int uniform_residues_impl(const int64_t *C, const int64_t *L, int n,
     return PG_OK;
 }
 
-// out[t*(n+1) + d] = coefficient d of per(C + x L) mod moduli[t], 2 <= n <= 32,
-// odd moduli 3 <= m < 2^30, k <= 65535.
+// out[t*(n+1) + d] = coefficient d of per(C + x L) mod moduli[t], 2 <= n <= 63
+// (orders above 32 in pg_poly_wide.cu), odd moduli 3 <= m < 2^30, k <= 65535.
 static int affine_residues_impl(const int64_t *C, const int64_t *L, int n,
                                 const uint64_t *moduli, int k, uint64_t *out) {
+    if (n > POLY_REG_MAX_N)
+        return affine_wide_residues(C, L, n, 0, 1ull << (n - 1), true, moduli, k, out);
 #if PG_POLY_UNIFORM
     if (rows_equal(C, n)) return uniform_residues_impl(C, L, n, moduli, k, out);
 #endif
@@ -390,7 +392,7 @@ static int affine_residues_impl(const int64_t *C, const int64_t *L, int n,
 extern "C" int pg_affine_residues(const int64_t *C, const int64_t *L, int n,
                                   const uint64_t *moduli, int k, uint64_t *out) {
     using namespace pg;
-    if (n < 0 || n > POLY_MAX_N) return fail(PG_ERANGE, "n must satisfy 0 <= n <= 32");
+    if (n < 0 || n > POLY_MAX_N) return fail(PG_ERANGE, "n must satisfy 0 <= n <= 63");
     if (k < 0) return fail(PG_EINVAL, "k must be non-negative");
     if (k == 0) return PG_OK;
     if (!moduli || !out || (n > 0 && (!C || !L))) return fail(PG_EINVAL, "null argument");

@@ -7,7 +7,11 @@
 
 namespace pg {
 
-constexpr int POLY_MAX_N = 32;
+constexpr int POLY_MAX_N = 63;
+// Largest order of the register kernels (pg_poly.cu, pg_poly_uniform.cu);
+// larger orders and Gray windows run the shared-memory kernel of
+// pg_poly_wide.cu.
+constexpr int POLY_REG_MAX_N = 32;
 
 struct PolyArgs {
     // general kernel: [k][N-1][2 dir][2 (C, L)][NP], (d - p) mod 2^32;
@@ -23,7 +27,14 @@ struct PolyArgs {
     volatile const int *abort_flag;
     uint64_t chunks;          // chunks per modulus
     int log_len;
+    uint64_t chunk0 = 0;      // first chunk (pg_poly_wide.cu windows)
 };
+
+// Glynn sums of per(C + x L) over the chunk-aligned Gray states [lo, hi)
+// modulo odd moduli < 2^30, orders 2..63 (pg_poly_wide.cu); `whole` also
+// scales by 2^(1-n).
+int affine_wide_residues(const int64_t *C, const int64_t *L, int n, uint64_t lo, uint64_t hi,
+                         bool whole, const uint64_t *moduli, int k, uint64_t *out);
 
 // From order 20 on the n+1 coefficient accumulators move from registers to
 // shared memory (one word per coefficient and thread, thread-minor so a warp

@@ -65,6 +65,9 @@ SIGNATURES = {
     "pg_permanent_mod3_cols": ([_c_u64p, _c_u64p, ctypes.c_int, _c_intp], ctypes.c_int),
     "pg_affine_residues": ([_c_i64p, _c_i64p, ctypes.c_int, _c_u64p, ctypes.c_int, _c_u64p],
                            ctypes.c_int),
+    "pg_affine_residues_partial": ([_c_i64p, _c_i64p, ctypes.c_int, ctypes.c_uint64,
+                                    ctypes.c_uint64, _c_u64p, ctypes.c_int, _c_u64p],
+                                   ctypes.c_int),
     "pg_binary_residues": ([_c_u8p, ctypes.c_int, _c_u64p, ctypes.c_int, _c_u64p], ctypes.c_int),
     "pg_exact_permanent": ([_c_i64p, ctypes.c_int, _c_u32p, ctypes.c_int], ctypes.c_int),
     "pg_exact_supported": ([_c_i64p, ctypes.c_int], ctypes.c_int),
@@ -89,6 +92,8 @@ SIGNATURES = {
                           ctypes.c_int, _c_intp], ctypes.c_int),
     "pg_glynn_c64_dev": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "pg_glynn_window": ([_c_f64p, _c_f64p, ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64,
+                         _c_f64p, _c_f64p, _c_f64p], ctypes.c_int),
     "pg_glynn_f64_dev": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
 }
@@ -263,7 +268,7 @@ def permanent_mod3_cols(col_mags, col_sgns, n: int) -> int:
 
 def affine_residues(constant, linear, moduli) -> list[list[int]]:
     """[coefficients of per(C + x L) mod m for m in moduli] (odd m < 2^30,
-    int64 entries, order <= 32)."""
+    int64 entries, order <= 63)."""
     c = np.ascontiguousarray(constant, dtype=np.int64)
     l = np.ascontiguousarray(linear, dtype=np.int64)
     n = c.shape[0] if c.ndim == 2 else 0
@@ -272,6 +277,21 @@ def affine_residues(constant, linear, moduli) -> list[list[int]]:
     check(load().pg_affine_residues(ptr(c, ctypes.c_int64), ptr(l, ctypes.c_int64), n,
                                     ptr(mods, ctypes.c_uint64), len(mods),
                                     ptr(out, ctypes.c_uint64)))
+    return [[int(x) for x in row] for row in out]
+
+
+def affine_residues_partial(constant, linear, lo: int, hi: int, moduli) -> list[list[int]]:
+    """[coefficients of the unscaled Glynn sum of per(C + x L) over Gray
+    states [lo, hi) mod m for m in moduli] (pg_affine_residues_partial)."""
+    c = np.ascontiguousarray(constant, dtype=np.int64)
+    l = np.ascontiguousarray(linear, dtype=np.int64)
+    n = c.shape[0]
+    mods = np.ascontiguousarray(np.asarray(list(moduli), dtype=np.uint64))
+    out = np.zeros((len(mods), n + 1), dtype=np.uint64)
+    check(load().pg_affine_residues_partial(ptr(c, ctypes.c_int64), ptr(l, ctypes.c_int64), n,
+                                            ctypes.c_uint64(lo), ctypes.c_uint64(hi),
+                                            ptr(mods, ctypes.c_uint64), len(mods),
+                                            ptr(out, ctypes.c_uint64)))
     return [[int(x) for x in row] for row in out]
 
 

@@ -6,6 +6,11 @@
                                  (perm_float.py:353-370), real matrices
     permanent_gpu(A)             numpy API of perm_parallel.permanent_gpu
                                  (perm_parallel.py:104-164), real matrices
+    glynn_window(A, lo, hi)      Glynn sum over a Gray window (one matrix)
+
+Orders up to 32 run the forward and the gradient in one traversal; orders
+33..63 run the forward only (two rows per lane), as the reference's
+permanent_parallel_real / _complex accept n <= 63.
 
 The forward and the gradient d per / d a_ij = per(A without row i, column j)
 come out of one Glynn traversal (pg_glynn_f64_dev).  The backward of the
@@ -45,6 +50,9 @@ def permanent_f64(A, want_grad: bool = True):
     batch = 1
     for d in lead:
         batch *= int(d)
+    if want_grad and n > 32:
+        raise ValueError("the FP64 gradient supports n <= 32 (the forward runs up to n = 63: "
+                         "want_grad=False)")
     Ab = A.reshape(batch, n, n).contiguous()
     per = torch.empty(batch, dtype=torch.float64, device=A.device)
     abs_sum = torch.empty_like(per)
@@ -148,6 +156,27 @@ def permanent_c64(A):
                                                 pr.data_ptr(), pi.data_ptr(), s.data_ptr(),
                                                 stream or None))
     return torch.complex(pr, pi).reshape(lead), s.reshape(lead)
+
+
+def glynn_window(matrix, lo: int, hi: int):
+    """(sum, abs_sum): the Glynn sum over Gray states [lo, hi) of a real or
+    complex square matrix (2 <= n <= 63), not divided by 2^(n-1), and the
+    sum of |terms| over the same states (pg_glynn_window).  Window sums of
+    a partition of [0, 2^(n-1)) add up to 2^(n-1) per(A)."""
+    a = np.asarray(matrix)
+    if a.ndim != 2 or a.shape[0] != a.shape[1]:
+        raise ValueError("Expected a square 2-D matrix")
+    n = a.shape[0]
+    re = np.ascontiguousarray(a.real, dtype=np.float64)
+    im = np.ascontiguousarray(a.imag, dtype=np.float64) if np.iscomplexobj(a) else None
+    out = np.zeros(3, dtype=np.float64)
+    f64p = ctypes.POINTER(ctypes.c_double)
+    _lib.check(_lib.load().pg_glynn_window(
+        re.ctypes.data_as(f64p), im.ctypes.data_as(f64p) if im is not None else None, n,
+        lo, hi, out[0:].ctypes.data_as(f64p), out[1:].ctypes.data_as(f64p),
+        out[2:].ctypes.data_as(f64p)))
+    total = complex(out[0], out[1]) if im is not None else float(out[0])
+    return total, float(out[2])
 
 
 def permanent_float(matrix):

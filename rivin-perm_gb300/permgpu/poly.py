@@ -35,7 +35,7 @@ _INT64_MAX = (1 << 63) - 1
 _INT32_MAX = (1 << 31) - 1
 # largest odd modulus the affine kernel takes (lazy sums stay below p * 2^32)
 GPU_MODULUS_LIMIT = 1 << 30
-GPU_MAX_ORDER = 32
+GPU_MAX_ORDER = 63
 
 Matrix = Tuple[Tuple[int, ...], ...]
 

@@ -104,3 +104,55 @@ def test_wide_modulus_goes_through_the_exact_vector():
     exact = permgpu.affine_permanent(c, l)
     for m in (3_037_000_501, (1 << 63) - 1):
         assert permgpu.affine_permanent_mod(c, l, m) == tuple(v % m for v in exact)
+
+
+@pytest.mark.parametrize("n", [3, 9, 20, 33])
+def test_window_kernel_whole_walks_vs_oracle(lib, n):
+    # the shared-memory kernel (orders above 32 and every window) over whole
+    # walks at small orders, and over a window at 33, against the oracle
+    rng = np.random.default_rng(970 + n)
+    c = rng.integers(-(1 << 40), 1 << 40, (n, n))
+    l = rng.integers(-9, 10, (n, n))
+    states = 1 << (n - 1)
+    lo, hi = (0, states) if n <= 20 else (states // 3 & ~63, (states // 3 & ~63) + (1 << 16))
+    got = lib.affine_residues_partial(c, l, lo, hi, MODULI)
+    for m, row in zip(MODULI, got):
+        assert row == oracle.affine_range_mod_p(c, l, m, lo, hi), (n, m)
+
+
+@pytest.mark.parametrize("n", [34, 40, 63])
+def test_windows_at_large_orders(lib, n):
+    # the reference accepts orders below 64 (perm_polynomial.py:151); whole
+    # walks at these orders take hours per modulus, so windows of 2^16
+    # states at the start, the middle and the end are checked against the
+    # oracle's window sums, for a general C and for C = J (rook form)
+    rng = np.random.default_rng(990 + n)
+    l = (rng.random((n, n)) < 0.5).astype(np.int64)
+    states, w = 1 << (n - 1), 1 << 16
+    for c in (rng.integers(-5, 6, (n, n)), np.ones((n, n), dtype=np.int64)):
+        for lo in (0, states // 2 + (1 << 20), states - w):
+            got = lib.affine_residues_partial(c, l, lo, lo + w, MODULI[3:])
+            for m, row in zip(MODULI[3:], got):
+                assert row == oracle.affine_range_mod_p(c, l, m, lo, lo + w), (n, lo, m)
+
+
+def test_rook_polynomial_order_34_whole_walk(lib):
+    # one whole 2^33-state evaluation above the register kernels' range: the
+    # exact rook polynomial of a sparse 34 x 34 0/1 matrix (the reference's
+    # rook_polynomial, perm_polynomial.py:1288-1411, accepts any order below
+    # 64), checked by identities that need no polynomial oracle: r_0 = 1,
+    # r_1 = number of ones, r_34 = per(A) from the exact engine, and
+    # sum_k r_k (34-k)! t^k = per(J + tA) for t = 1, 2 from the exact engine
+    import permgpu
+    rng = np.random.default_rng(3434)
+    n = 34
+    a = (rng.random((n, n)) < 0.15).astype(np.int64)
+    np.fill_diagonal(a, 1)
+    r = permgpu.rook_polynomial(a.tolist())
+    assert len(r) == n + 1
+    assert r[0] == 1 and r[1] == int(a.sum())
+    assert r[n] == lib.exact_permanent(a, lib.exact_limbs(a))
+    for t in (1, 2):
+        m = np.ones((n, n), dtype=np.int64) + t * a
+        want = lib.exact_permanent(m, lib.exact_limbs(m))
+        assert sum(rk * math.factorial(n - k) * t ** k for k, rk in enumerate(r)) == want

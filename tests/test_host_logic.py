@@ -205,4 +205,4 @@ def test_fp64_entries_handle_orders_below_two_on_the_host():
     per, s = _lib.glynn_c64(np.zeros((2, 0, 0), dtype=np.complex128))
     assert per.tolist() == [1, 1]
     with pytest.raises(_lib.PermGpuError, match="PG_ERANGE"):
-        _lib.glynn_c64(np.zeros((1, 33, 33), dtype=np.complex128))
+        _lib.glynn_c64(np.zeros((1, 64, 64), dtype=np.complex128))
