@@ -3,7 +3,7 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
                     [--workload generic32|generic24|batch4096|float28|schur|schur41|
-                                binary40|grid40|rook28|mod3_40] [--no-cpu]
+                                binary40|grid40|rook28|mod3_40|split36] [--no-cpu]
 
 The default workload is generic32 (below); the others print their own
 metric line (batched exact permanents, FP64 forward+gradient, Schur
@@ -27,7 +27,9 @@ count for this matrix.
 Multi-GPU (torchrun, WORLD_SIZE > 1): every rank evaluates its own seeded
 matrix (replicas of the workload; the units are independent matrices), a
 barrier brackets the timed region, the max time over ranks is taken and
-`value` is the total over ranks ("scaling": "weak").
+`value` is the total over ranks ("scaling": "weak").  --workload split36
+instead splits ONE permanent across the ranks by Gray range and gathers
+the partial words ("scaling": "strong").
 """
 
 from __future__ import annotations
@@ -143,6 +145,28 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def host_info() -> dict:
+    """The CPU model and the C compiler that built the CPU baseline."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.split(":")[0].strip() in ("Model name", "Model"):
+                model = line.split(":", 1)[1].strip()
+                if line.startswith("Model name"):
+                    break
+    except (OSError, subprocess.TimeoutExpired):
+        pass
+    try:
+        cc = subprocess.run(["gcc", "--version"], capture_output=True, text=True,
+                            timeout=10).stdout.splitlines()[0]
+    except (OSError, subprocess.TimeoutExpired, IndexError):
+        cc = None
+    import platform
+    return {"cpu_model": model, "machine": platform.machine(), "compiler": cc,
+            "flags": "-O3 -fopenmp"}
+
+
 def cpu_sample(matrix, seconds_target: float = 12.0):
     """Time the reference's Glynn residue loop on the host cores over a
     bounded prefix of the Gray walk.  Returns (states/s for one prime, cores,
@@ -214,7 +238,7 @@ def run_reference(args, world, rank):
         "config": {"workload": f"{args.workload}: {desc}", "n": n, "crt_primes": k_ref},
         "time_to_exact_s": (1 << (n - 1)) / value,
         "cpu_baseline": {"value": value, "unit": "steps/s", "cores": threads,
-                         "kind": "port", "sample": sample},
+                         "kind": "port", "sample": sample, "host": host_info()},
         "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -370,7 +394,7 @@ def run_gpu(args, world, rank, local):
                                              "mad.wide.u32": peak_madw}},
             "cpu_baseline": None if cpu_rate is None else {
                 "value": cpu_rate, "unit": "steps/s", "cores": cores, "kind": kind,
-                "sample": sample},
+                "sample": sample, "host": host_info()},
             "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_step},
             "clocks": clk,
@@ -378,6 +402,67 @@ def run_gpu(args, world, rank, local):
         }
         print(json.dumps(line))
     plan.close()
+
+
+def run_gpu_split(args, world, rank, local):
+    """split36: ONE exact permanent (36x36 int64, entries U[-8,8], numpy
+    default_rng(36)) split across the ranks by Gray range: each rank walks
+    shard.state_range(n, rank, world) on its GPU through pg_exact_partial,
+    the partial words are all-gathered (torch.distributed) and every rank
+    combines the same exact value.  Total work is fixed as ranks are added
+    ("scaling": "strong").  Each step is timed on the host around the whole
+    call (table upload, kernel, read-back, exchange, combine), so value and
+    e2e coincide."""
+    import torch
+    from permgpu import _lib, shard, workloads
+    torch.cuda.set_device(local)
+    n = args.split_order
+    a = workloads.generic_matrix(n, n)
+    states = 1 << (n - 1)
+    lo, hi = shard.state_range(n, rank, world)
+    gather = shard.torch_gather if world > 1 else (lambda w: [list(w)])
+    for _ in range(args.warmup):
+        got = shard.split_exact_permanent(a, rank, world, gather=gather)
+    checked = None
+    if rank == 0:
+        # independent check: per(A) modulo two primes from the residue kernel
+        primes = [2_147_483_647, 2_147_483_629]
+        if _lib.residues(a, primes) != [got % q for q in primes]:
+            raise SystemExit("split36: combined value disagrees with the residue kernel")
+        checked = "per(A) mod 2147483647 and 2147483629 from the residue kernel (pg_residues)"
+    clocks = ClockSampler(local).start()
+    ts = []
+    for _ in range(args.steps):
+        barrier(world)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        v = shard.split_exact_permanent(a, rank, world, gather=gather)
+        ts.append(time.perf_counter() - t)
+        if v != got:
+            raise SystemExit("split36: results changed between steps")
+    barrier(world)
+    clk = clocks.stop()
+    step_s = max_over_ranks(world, statistics.mean(ts))
+    if rank == 0:
+        print(json.dumps({
+            "metric": f"Glynn steps/s (one exact per(A), n={n} int, split by Gray range)",
+            "value": states / step_s, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * step_s, "higher_is_better": True,
+            "scaling": "strong", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+            "config": {"workload": f"split36: one {n}x{n} int64 matrix, entries U[-8,8], numpy "
+                                   f"default_rng({n}); rank r walks Gray states "
+                                   f"state_range(n, r, {world})", "states": states,
+                       "rank0_range": [lo, hi], "exchange": "torch.distributed all_gather of "
+                                                            f"{shard.GATHER_WIDTH} int64 words",
+                       "l2": "inputs ~10 KiB; compute-bound"},
+            "time_to_exact_s": step_s, "result": str(got),
+            "result_checked_against_reference": checked is not None, "result_check": checked,
+            "e2e": {"value": states / step_s, "unit": "steps/s",
+                    "h2d_bytes_per_step": (n - 1) * 2 * ((n + 3) & ~3) * 4,
+                    "d2h_bytes_per_step": 8 * shard.GATHER_WIDTH,
+                    "note": "whole call timed on the host (value and e2e coincide)"},
+            "clocks": clk, "gpu_launches": args.steps,
+        }))
 
 
 def run_gpu_batch(args, world, rank, local):
@@ -948,7 +1033,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="generic32",
                     choices=sorted(WORKLOADS) + ["batch4096", "float28", "schur", "schur41",
-                                                 "binary40", "grid40", "rook28", "mod3_40"])
+                                                 "binary40", "grid40", "rook28", "mod3_40",
+                                                 "split36"])
     ap.add_argument("--residue-loop-sample", type=int, default=256)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -956,6 +1042,8 @@ def main():
                     help="float28: matrices per step (256 is the workload; smaller for profiling)")
     ap.add_argument("--order", type=int, default=41,
                     help="schur41: prime Schur order (41 is the workload; 37 for profiling)")
+    ap.add_argument("--split-order", type=int, default=36,
+                    help="split36: order of the one split permanent (36 is the workload)")
     ap.add_argument("--mod3-order", type=int, default=40,
                     help="mod3_40: matrix order (40 is the workload; smaller for profiling)")
     args = ap.parse_args()
@@ -964,6 +1052,8 @@ def main():
         run_reference(args, world, rank)
     elif args.workload == "batch4096":
         run_gpu_batch(args, world, rank, local)
+    elif args.workload == "split36":
+        run_gpu_split(args, world, rank, local)
     elif args.workload == "float28":
         run_gpu_float28(args, world, rank, local)
     elif args.workload in ("schur", "schur41", "binary40", "grid40"):

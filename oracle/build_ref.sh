@@ -5,9 +5,13 @@
 # used only as the CPU checker, the golden-vector generator and the CPU
 # baseline; no reference source is copied into this repository.
 #
-# usage: oracle/build_ref.sh [REFERENCE_DIR]   (default /root/reference)
+# usage: oracle/build_ref.sh REFERENCE_DIR   (the rivin-perm checkout)
 set -euo pipefail
-REF="${1:-/root/reference}"
+if [ $# -ne 1 ]; then
+  echo "usage: $0 REFERENCE_DIR" >&2
+  exit 2
+fi
+REF="$1"
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
 OUT="$HERE/_ref"
 if [ ! -f "$REF/perm_c_omp.c" ]; then

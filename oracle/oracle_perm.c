@@ -75,6 +75,21 @@ int or_max_threads(void) {
 #endif
 }
 
+/* Largest modulus whose residue products fit a signed 64-bit product: the
+ * reference multiplies row sums with a plain 64-bit (a * b) % p up to it and
+ * with 128-bit arithmetic above (perm_c_omp.c:36-47 selector). */
+#define OR_DIRECT_MUL_LIMIT INT64_C(3037000499)
+
+static inline int64_t row_product(const int64_t *rs, int n, int64_t p) {
+    int64_t prod = 1 % p;
+    if (p <= OR_DIRECT_MUL_LIMIT) {
+        for (int r = 0; r < n; r++) prod = (prod * rs[r]) % p;
+    } else {
+        for (int r = 0; r < n; r++) prod = mul_mod(prod, rs[r], p);
+    }
+    return prod;
+}
+
 /* Glynn over states [lo, hi) of the 2^(n-1) fixed-last-sign Gray walk.
  * Entries of m are in [0, p).  Returns the signed partial sum mod p. */
 static int64_t glynn_block(const int64_t *m, int n, int64_t p,
@@ -103,8 +118,7 @@ static int64_t glynn_block(const int64_t *m, int n, int64_t p,
             }
             sign = -sign;
         }
-        int64_t prod = 1 % p;
-        for (int r = 0; r < n; r++) prod = mul_mod(prod, rs[r], p);
+        const int64_t prod = row_product(rs, n, p);
         acc = sign < 0 ? sub_mod(acc, prod, p) : add_mod(acc, prod, p);
     }
     return acc;

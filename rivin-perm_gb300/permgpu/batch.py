@@ -53,7 +53,8 @@ def batch_permanents(matrices: Sequence, tune="auto", cache_path=None) -> List[i
                 out[i] = v
         finally:
             plan.close()
+    in_batch = set(ok)
     for i, m in enumerate(mats):
-        if i not in set(ok):
+        if i not in in_batch:
             out[i] = matrix_permanent(m.tolist())
     return out

@@ -70,44 +70,84 @@ def row_masks(matrix) -> List[int]:
     return [sum(1 << j for j, v in enumerate(row) if v) for row in matrix]
 
 
+def _bits(mask: int):
+    while mask:
+        low = mask & -mask
+        yield low.bit_length() - 1
+        mask ^= low
+
+
 def perfect_matching(masks: Sequence[int]) -> Optional[List[int]]:
-    """Row -> column perfect matching by BFS augmenting paths, or None."""
+    """Row -> column perfect matching of the 0/1 matrix with row bitmasks
+    `masks`, or None when there is none.
+
+    Hopcroft-Karp in phases: a breadth-first pass from all unmatched rows at
+    once assigns every row its alternating-path layer (row -> any column of
+    the row -> the row matched to that column); a depth-first pass then
+    augments a maximal set of vertex-disjoint paths that climb the layers
+    and end at an unmatched column.  Each phase lengthens the shortest
+    augmenting path, so O(sqrt(n)) phases suffice.
+    """
     n = len(masks)
-    match_row, match_col = [-1] * n, [-1] * n
-    for root in range(n):
-        parent = [-1] * n            # column -> row that reached it
-        seen_col = [False] * n
-        queue, head, free = [root], 0, -1
-        visited_row = [False] * n
-        visited_row[root] = True
-        while head < len(queue) and free < 0:
-            r = queue[head]
-            head += 1
-            m = masks[r]
-            while m:
-                low = m & -m
-                c = low.bit_length() - 1
-                m ^= low
-                if seen_col[c]:
+    col_of = [-1] * n            # row -> matched column
+    row_of = [-1] * n            # column -> matched row
+    while True:
+        free_rows = [r for r in range(n) if col_of[r] < 0]
+        if not free_rows:
+            return col_of
+        layer = [-1] * n
+        for r in free_rows:
+            layer[r] = 0
+        frontier, open_cols, reached = free_rows, (1 << n) - 1, False
+        while frontier and not reached:
+            nxt = []
+            for r in frontier:
+                hit = masks[r] & open_cols
+                open_cols &= ~hit
+                for c in _bits(hit):
+                    m = row_of[c]
+                    if m < 0:
+                        reached = True
+                    elif layer[m] < 0:
+                        layer[m] = layer[r] + 1
+                        nxt.append(m)
+            frontier = nxt
+        if not reached:
+            return None          # some row can reach no unmatched column
+        todo = list(masks)       # columns each row has not tried yet
+        grew = False
+        for root in free_rows:
+            rows, cols = [root], []
+            while rows:
+                r = rows[-1]
+                step = None
+                while todo[r]:
+                    low = todo[r] & -todo[r]
+                    todo[r] ^= low
+                    c = low.bit_length() - 1
+                    m = row_of[c]
+                    if m < 0 or layer[m] == layer[r] + 1:
+                        step = (c, m)
+                        break
+                if step is None:             # dead end: never revisit r
+                    layer[r] = -1
+                    rows.pop()
+                    if cols:
+                        cols.pop()
                     continue
-                seen_col[c] = True
-                parent[c] = r
-                if match_col[c] < 0:
-                    free = c
-                    break
-                nr = match_col[c]
-                if not visited_row[nr]:
-                    visited_row[nr] = True
-                    queue.append(nr)
-        if free < 0:
-            return None
-        c = free
-        while c >= 0:
-            r = parent[c]
-            prev = match_row[r]
-            match_row[r], match_col[c] = c, r
-            c = prev
-    return match_row
+                c, m = step
+                cols.append(c)
+                if m >= 0:
+                    rows.append(m)
+                    continue
+                for rr, cc in zip(rows, cols):   # flip the path
+                    col_of[rr], row_of[cc] = cc, rr
+                for rr in rows:                  # vertex-disjoint paths per phase
+                    layer[rr] = -1
+                grew = True
+                break
+        if not grew:
+            raise RuntimeError("matching phase found a free column but no augmenting path")
 
 
 def strong_components(adj: Sequence[Sequence[int]]) -> List[List[int]]:
@@ -163,28 +203,31 @@ def strong_components(adj: Sequence[Sequence[int]]) -> List[List[int]]:
 def matching_blocks(masks: Sequence[int]) -> Tuple[bool, List[List[List[int]]]]:
     """(feasible, blocks): independent square 0/1 blocks whose permanents
     multiply to per(A); an infeasible matrix (no perfect matching) has
-    permanent 0."""
+    permanent 0.
+
+    The blocks are the fine decomposition of the bipartite graph: with a
+    perfect matching fixed, orient every unmatched edge row -> column and
+    every matched edge both ways; an edge lies on some perfect matching
+    exactly when its ends share a strongly connected component, so the
+    components (rows with their matched columns) are the blocks and every
+    edge between components is in no perfect matching.  The decomposition
+    does not depend on which perfect matching was found.
+    """
     n = len(masks)
     match = perfect_matching(masks)
     if match is None:
         return False, []
     if n == 0:
         return True, []
-    col_to_row = [-1] * n
-    for r, c in enumerate(match):
-        col_to_row[c] = r
-    adj = []
-    for m in masks:
-        targets = []
-        while m:
-            low = m & -m
-            targets.append(col_to_row[low.bit_length() - 1])
-            m ^= low
-        adj.append(targets)
+    adj: List[List[int]] = [[] for _ in range(2 * n)]   # rows 0..n-1, columns n..2n-1
+    for r, mask in enumerate(masks):
+        adj[n + match[r]].append(r)
+        adj[r].extend(n + c for c in _bits(mask))
     blocks = []
     for comp in strong_components(adj):
-        cols = [match[r] for r in comp]
-        blocks.append([[(masks[r] >> c) & 1 for c in cols] for r in comp])
+        rows = [v for v in comp if v < n]
+        cols = sorted(match[r] for r in rows)
+        blocks.append([[(masks[r] >> c) & 1 for c in cols] for r in rows])
     return True, blocks
 
 

@@ -11,7 +11,9 @@ and the exchange is a host-level gather of a few 64-bit words per rank.
     all = gather(words)                              # any transport
     per = combine_exact_words(all, n)
 
-The same split works for residues (combine_residues).
+split_exact_permanent runs these steps on one rank with a torch.distributed
+all-gather as the transport.  The same split works for residues
+(combine_residues).
 """
 
 from __future__ import annotations
@@ -82,3 +84,32 @@ def combine_residues(partials: Iterable[int], p: int, n: int) -> int:
     total = sum(int(x) for x in partials) % p
     inv2 = (p + 1) // 2
     return total * pow(inv2, n - 1, p) % p
+
+
+GATHER_WIDTH = 32      # words per rank in the exchange (NL <= 18 for every shape)
+
+
+def torch_gather(words: Sequence[int], group=None) -> List[List[int]]:
+    """All-gather one rank's partial words over torch.distributed (host
+    tensors for gloo, device tensors for nccl); returns every rank's words."""
+    import torch
+    import torch.distributed as dist
+    if len(words) > GATHER_WIDTH:
+        raise ValueError("too many partial words for the exchange")
+    dev = "cuda" if dist.get_backend(group) == "nccl" else "cpu"
+    t = torch.tensor(list(words) + [0] * (GATHER_WIDTH - len(words)), dtype=torch.int64,
+                     device=dev)
+    out = [torch.zeros_like(t) for _ in range(dist.get_world_size(group))]
+    dist.all_gather(out, t, group=group)
+    return [o.cpu().tolist() for o in out]
+
+
+def split_exact_permanent(matrix, rank: int, world: int, gather=torch_gather,
+                          partial=exact_partial_words) -> int:
+    """per(A) of one matrix split across `world` ranks: this rank walks its
+    Gray range on its GPU (`partial`), the words are exchanged (`gather`,
+    any transport), and every rank combines the same exact value."""
+    n = len(matrix)
+    lo, hi = state_range(n, rank, world)
+    words = partial(matrix, lo, hi)
+    return combine_exact_words(gather(words), n)

@@ -3,8 +3,8 @@
 Run in a checkout that has the reference (rivin-perm) at REFERENCE_DIR and
 its OpenMP extensions built by oracle/build_ref.sh:
 
-    oracle/build_ref.sh /root/reference
-    python tests/golden/make_golden.py [--reference /root/reference] [--slow]
+    oracle/build_ref.sh REFERENCE_DIR
+    python tests/golden/make_golden.py --reference REFERENCE_DIR [--slow]
 
 Every value is produced by the reference's own code: perm_c_ext /
 perm_binary_ext (compiled from perm_c_omp.c / perm_binary_omp.c) and the
@@ -38,7 +38,8 @@ def dump(name, obj):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", required=True,
+                    help="the rivin-perm checkout the fixtures are generated from")
     ap.add_argument("--slow", action="store_true")
     ap.add_argument("--necklace-only", action="store_true",
                     help="regenerate only necklace_stats.json")

@@ -206,3 +206,34 @@ def test_fp64_entries_handle_orders_below_two_on_the_host():
     assert per.tolist() == [1, 1]
     with pytest.raises(_lib.PermGpuError, match="PG_ERANGE"):
         _lib.glynn_c64(np.zeros((1, 64, 64), dtype=np.complex128))
+
+
+def test_matching_and_blocks_against_brute_force():
+    # Hopcroft-Karp matching and the strongly-connected block split on every
+    # kind of small 0/1 matrix: the matching is perfect whenever per(A) > 0,
+    # absent when per(A) = 0, and the block permanents multiply to per(A)
+    import itertools
+    import random
+    from permgpu import binary as pb
+
+    def brute(a):
+        k = len(a)
+        return sum(all(a[i][p[i]] for i in range(k)) for p in itertools.permutations(range(k)))
+
+    rng = random.Random(2024)
+    for _ in range(1500):
+        k = rng.randint(0, 7)
+        dens = rng.random()
+        a = [[1 if rng.random() < dens else 0 for _ in range(k)] for _ in range(k)]
+        masks = pb.row_masks(a)
+        want = brute(a)
+        m = pb.perfect_matching(masks)
+        if m is None:
+            assert want == 0
+        else:
+            assert sorted(m) == list(range(k)) and all(a[r][m[r]] for r in range(k))
+        feasible, blocks = pb.matching_blocks(masks)
+        assert (math.prod(brute(b) for b in blocks) if feasible else 0) == want
+        if feasible:
+            assert sum(len(b) for b in blocks) == k
+            assert all(brute(b) > 0 for b in blocks)

@@ -75,10 +75,20 @@ def _worker(rank, world, port, q):
         wl = [torch.zeros_like(wt) for _ in range(world)]
         dist.all_gather(wl, wt)
         exact = shard.combine_exact_words([w.tolist() for w in wl], n)
+        # the single-permanent split of bench.py's split workload: the same
+        # product function, with the Python partial standing in for the
+        # rank's GPU and the torch.distributed gather over gloo
+        def stand_in(m, lo_, hi_):
+            S_ = _exact_partial_python(m, lo_, hi_)
+            w = [(S_ >> (32 * k)) & 0xffffffff for k in range(8)]
+            w[-1] = S_ >> (32 * 7)
+            return w
+        split = shard.split_exact_permanent(a, rank, world, partial=stand_in)
         bench.barrier(world)
         mx = bench.max_over_ranks(world, float(rank + 1))
         if rank == 0:
-            q.put((res, exact, mx, oracle.permanent_mod_p(a, p, 1), oracle.exact_permanent(a)))
+            q.put((res, exact, mx, oracle.permanent_mod_p(a, p, 1), oracle.exact_permanent(a),
+                   split))
     finally:
         dist.destroy_process_group()
 
@@ -94,9 +104,10 @@ def test_two_rank_sharded_glynn_over_gloo():
     for p in procs:
         p.join(timeout=240)
         assert p.exitcode == 0
-    res, exact, mx, want_res, want_exact = q.get(timeout=10)
+    res, exact, mx, want_res, want_exact, split = q.get(timeout=10)
     assert res == want_res
     assert exact == want_exact
+    assert split == want_exact
     assert mx == 2.0
 
 
