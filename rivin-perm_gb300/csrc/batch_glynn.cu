@@ -42,6 +42,7 @@ struct BatchArgs {
     const uint64_t *table_off;    // int32 offset of each matrix's table
     const uint8_t *orders;        // n per matrix
     const uint8_t *groups;        // row-group size G per matrix
+    const uint8_t *frows;         // float rows per group (0 or 3) per matrix
     const uint8_t *log_len;       // chunk log length per matrix
     const uint64_t *chunks;       // chunks per matrix
     const BatchTask *tasks;
@@ -60,8 +61,22 @@ __host__ __device__ constexpr bool batch_compiled(int N, int G) {
            : N < 4 ? G == N
            : G == 4 || (G == 5 && N >= 20);
 }
+// Float rows (exact_glynn.cuh): three of each group's rows as exact FP32
+// sums, so a group of 4 costs one IMUL instead of three.  Compiled for
+// groups of 4 at orders 20, 24 and 28 (where the batch's time goes); a
+// matrix of order 21..27 whose rows qualify runs at the next of these
+// orders with constant rows s = 1 added (zero table entries), which leaves
+// its walk, its permanent and its product words unchanged.  Other float-row
+// shapes made the shared kernel spill.
+__host__ __device__ constexpr bool batch_frows_compiled(int N, int G) {
+    return (N == 20 || N == 24 || N == 28) && G == 4;
+}
+constexpr int BATCH_FROWS = 3;
+__host__ __device__ constexpr int batch_frows_order(int n) {
+    return n >= 20 && n <= 28 ? (n + 3) & ~3 : 0;
+}
 
-template <int N, int G>
+template <int N, int G, int FR = 0>
 __device__ __forceinline__ void batch_task(const int32_t *wtab, const BatchArgs &a,
                                            const BatchTask &t, int lane) {
     using S = ExactShape<N, G>;
@@ -80,8 +95,8 @@ __device__ __forceinline__ void batch_task(const int32_t *wtab, const BatchArgs 
     bool ok = true;
     if (cb < ce) {
         int32_t s[N];
-        exact_init<N>(wtab, wtab + (N - 1) * 2 * NP, s, cb << log_len);
-        ok = exact_walk<N, G>(wtab, s, acc, cb, ce, log_len, a.abort_flag);
+        exact_init<N, G, FR>(wtab, wtab + (N - 1) * 2 * NP, s, cb << log_len);
+        ok = exact_walk<N, G, FR>(wtab, s, acc, cb, ce, log_len, a.abort_flag);
     }
     if (!ok) atomicExch(a.status, 1);
 #pragma unroll
@@ -115,8 +130,11 @@ __global__ void __launch_bounds__(256, 2) batch_glynn_kernel(BatchArgs a) {
             __syncwarp();
             cur = t.m;
         }
-        switch (n * 8 + a.groups[t.m]) {
-#define PG_BATCH_CASE(NN, GG) case NN * 8 + GG: batch_task<NN, GG>(wtab, a, t, lane); break;
+        switch (n * 16 + a.groups[t.m] * 2 + (a.frows[t.m] ? 1 : 0)) {
+#define PG_BATCH_CASE(NN, GG) \
+    case NN * 16 + GG * 2: batch_task<NN, GG>(wtab, a, t, lane); break;
+#define PG_BATCH_FCASE(NN, GG) \
+    case NN * 16 + GG * 2 + 1: batch_task<NN, GG, BATCH_FROWS>(wtab, a, t, lane); break;
             PG_BATCH_CASE(2, 2) PG_BATCH_CASE(3, 3)
 #define PG_BATCH_G4(NN) PG_BATCH_CASE(NN, 4)
 #define PG_BATCH_G5(NN) PG_BATCH_CASE(NN, 5)
@@ -130,8 +148,12 @@ __global__ void __launch_bounds__(256, 2) batch_glynn_kernel(BatchArgs a) {
             PG_BATCH_G5(21) PG_BATCH_G5(22) PG_BATCH_G5(23) PG_BATCH_G5(24) PG_BATCH_G5(25)
             PG_BATCH_G5(26) PG_BATCH_G5(27) PG_BATCH_G5(28) PG_BATCH_G5(29) PG_BATCH_G5(30)
             PG_BATCH_G5(31) PG_BATCH_G5(32)
+#define PG_BATCH_F(NN) PG_BATCH_FCASE(NN, 4)
+            PG_BATCH_F(20) PG_BATCH_F(24) PG_BATCH_F(28)
+#undef PG_BATCH_F
 #undef PG_BATCH_G4
 #undef PG_BATCH_G5
+#undef PG_BATCH_FCASE
 #undef PG_BATCH_CASE
         default: break;
         }
@@ -177,6 +199,8 @@ struct BatchPlan {
     int count = 0;
     std::vector<int> orders;
     std::vector<uint8_t> groups;           // row-group size of each kernel matrix
+    std::vector<uint8_t> frows;            // float rows per group (0 or 3)
+    std::vector<uint8_t> korder;           // order the kernel runs (padded for float rows)
     std::vector<uint8_t> in_kernel;        // 1 if the batch kernel evaluates it
     std::vector<std::vector<int64_t>> external;  // matrices for the single engine
     std::vector<int> ext_index;
@@ -226,6 +250,8 @@ int pg_batch_plan_create(const int64_t *A, const int64_t *offsets, const int32_t
     P.orders.assign(orders, orders + count);
     P.in_kernel.assign(count, 0);
     P.groups.assign(count, 0);
+    P.frows.assign(count, 0);
+    P.korder.assign(count, 0);
     P.ext_index.assign(count, -1);
     P.bound_bits.assign(count, 0.0);
 
@@ -254,18 +280,51 @@ int pg_batch_plan_create(const int64_t *A, const int64_t *offsets, const int32_t
         }
         P.in_kernel[m] = 1;
         P.groups[m] = (uint8_t)G;
-        const int NP = (n + 3) & ~3;
+        // float rows at the padded order K: a bound-only K x K image whose
+        // extra rows have bound 1 picks the grouping and the float rows
+        int K = n, FR = 0;
+        const int KF = batch_frows_order(n);
+        if (G == 4 && batch_frows_compiled(KF, 4)) {
+            std::vector<int64_t> img((size_t)KF * KF, 0);
+            for (int i = 0; i < KF; i++)
+                for (int j = 0; j < KF; j++)
+                    img[(size_t)i * KF + j] = i < n ? (j < n ? a[(size_t)i * n + j] : 0) : (j == 0);
+            std::vector<uint64_t> Bk(KF);
+            for (int i = 0; i < KF; i++) {
+                uint64_t b = 0;
+                for (int j = 0; j < KF; j++) b += (uint64_t)std::llabs(img[(size_t)i * KF + j]);
+                Bk[i] = b;
+            }
+            std::vector<int> ko(KF);
+            if (exact_group_rows(Bk.data(), KF, 4, ko.data()) &&
+                exact_frows_arrange(img.data(), KF, 4, BATCH_FROWS, ko.data())) {
+                K = KF;
+                FR = BATCH_FROWS;
+                order = ko;
+            }
+        }
+        P.frows[m] = (uint8_t)FR;
+        P.korder[m] = (uint8_t)K;
+        const int NP = (K + 3) & ~3;
         toff[m] = tables.size();
         const size_t base = tables.size();
-        tables.resize(base + (size_t)(n - 1) * 2 * NP + NP, 0);
-        for (int ii = 0; ii < n; ii++) {
+        tables.resize(base + (size_t)(K - 1) * 2 * NP + NP, 0);
+        for (int ii = 0; ii < K; ii++) {
+            const bool fl = FR > 0 && exact_float_row(K, G, FR, ii);
+            const auto enc = [&](int64_t v) {
+                return fl ? (int32_t)exact_float_bits((float)v) : (int32_t)v;
+            };
+            if (order[ii] >= n) {          // added constant row: s = 1, no column
+                tables[base + (size_t)(K - 1) * 2 * NP + ii] = enc(1);
+                continue;
+            }
             const int64_t *row = a + (size_t)order[ii] * n;
             int64_t sum = 0;
             for (int j = 0; j < n; j++) sum += row[j];
-            tables[base + (size_t)(n - 1) * 2 * NP + ii] = (int32_t)sum;
+            tables[base + (size_t)(K - 1) * 2 * NP + ii] = enc(sum);
             for (int j = 0; j < n - 1; j++) {
-                tables[base + (size_t)(2 * j + 0) * NP + ii] = (int32_t)(2 * row[j]);
-                tables[base + (size_t)(2 * j + 1) * NP + ii] = (int32_t)(-2 * row[j]);
+                tables[base + (size_t)(2 * j + 0) * NP + ii] = enc(2 * row[j]);
+                tables[base + (size_t)(2 * j + 1) * NP + ii] = enc(-2 * row[j]);
             }
         }
         const int log_states = n - 1;
@@ -277,7 +336,7 @@ int pg_batch_plan_create(const int64_t *A, const int64_t *offsets, const int32_t
         uint64_t k = lane_log > ll ? (1ull << (lane_log - ll)) : 1;
         if (k * 32 > ch) k = (ch + 31) / 32;
         if (k < 1) k = 1;
-        ord8[m] = (uint8_t)n;
+        ord8[m] = (uint8_t)K;
         loglen[m] = (uint8_t)ll;
         nchunks[m] = ch;
         P.kernel_states += 1ull << log_states;
@@ -301,7 +360,8 @@ int pg_batch_plan_create(const int64_t *A, const int64_t *offsets, const int32_t
     const size_t off_toff = align_up(off_tables + tables.size() * 4, 256);
     const size_t off_ord = align_up(off_toff + (size_t)count * 8, 256);
     const size_t off_grp = align_up(off_ord + (size_t)count, 256);
-    const size_t off_ll = align_up(off_grp + (size_t)count, 256);
+    const size_t off_fr = align_up(off_grp + (size_t)count, 256);
+    const size_t off_ll = align_up(off_fr + (size_t)count, 256);
     const size_t off_nch = align_up(off_ll + (size_t)count, 256);
     const size_t off_tasks = align_up(off_nch + (size_t)count * 8, 256);
     P.off_acc = align_up(off_tasks + sorted.size() * sizeof(BatchTask), 256);
@@ -322,6 +382,7 @@ int pg_batch_plan_create(const int64_t *A, const int64_t *offsets, const int32_t
     std::memcpy(P.host + off_toff, toff.data(), (size_t)count * 8);
     std::memcpy(P.host + off_ord, ord8.data(), (size_t)count);
     if (count) std::memcpy(P.host + off_grp, P.groups.data(), (size_t)count);
+    if (count) std::memcpy(P.host + off_fr, P.frows.data(), (size_t)count);
     std::memcpy(P.host + off_ll, loglen.data(), (size_t)count);
     std::memcpy(P.host + off_nch, nchunks.data(), (size_t)count * 8);
     if (!sorted.empty())
@@ -339,6 +400,7 @@ int pg_batch_plan_create(const int64_t *A, const int64_t *offsets, const int32_t
     a.table_off = (const uint64_t *)(P.dev + off_toff);
     a.orders = (const uint8_t *)(P.dev + off_ord);
     a.groups = (const uint8_t *)(P.dev + off_grp);
+    a.frows = (const uint8_t *)(P.dev + off_fr);
     a.log_len = (const uint8_t *)(P.dev + off_ll);
     a.chunks = (const uint64_t *)(P.dev + off_nch);
     a.tasks = (const BatchTask *)(P.dev + off_tasks);
@@ -412,7 +474,7 @@ int pg_batch_plan_result(pg_batch_plan *plan, void *stream, uint32_t *out, int l
         const int W = BATCH_WORDS + 3;
         std::vector<uint32_t> S(W, 0);
         const int G = P.groups[m];
-        const int NL = (n + G - 1) / G + 1;
+        const int NL = (P.korder[m] + G - 1) / G + 1;   // words of the order the kernel ran
         for (int l = 0; l < NL; l++) add_i64_at(S, l, acc[(size_t)m * BATCH_WORDS + l]);
         const int sh = n - 1;
         for (int b = 0; b < sh; b++)

@@ -1,0 +1,292 @@
+// Exact Glynn kernel for 0/1 matrices: bit-sliced row counts, zero-row
+// skipping and warp-compacted exact evaluation.
+//
+// For a 0/1 matrix the Glynn row sum of state d is s_r = deg_r - 2 m_r,
+// where m_r counts the row's ones in columns whose sign is minus.  A term
+// is zero as soon as one row sum is zero (an even-degree row with
+// m_r = deg_r / 2), which for the benchmark matrices is most states
+// (40 x 40 Bernoulli(1/2): ~92 %; the 4x4x5 grid: ~99.9 %).  The reference
+// keeps int16 row sums, a zero counter and a ratio-updated product mod p
+// for every state (perm_binary_omp.c:236-347, perm_binary_cuda.cu:111-205);
+// this kernel instead keeps the counts t_r = deg_r - m_r bit-sliced: plane
+// b holds bit b of every row's count, one bit per row (two 32-bit words for
+// up to 64 rows).  A Gray step adds or subtracts 1 in the rows of the
+// toggled column: a ripple carry through the planes, two three-input
+// logic operations per plane and word.  The zero test compares the planes
+// with those of deg_r / 2 on the even-degree rows: one more per plane and
+// word.  Nothing is multiplied on the walk.
+//
+// States with no zero row are appended to a per-warp queue in shared memory
+// (a ballot gives each lane its slot).  Whenever 32 are queued, every lane
+// of the warp evaluates one of them exactly: the row sums from the state's
+// Gray word by popcount (s_r = deg_r - 2 popc(row_r & gray(g))), then the
+// exact multi-word term of exact_glynn.cuh (row groups, signed running
+// product, 64-bit column accumulators).  Walk and evaluation are both
+// warp-uniform, so no lane idles while another evaluates.
+//
+// Rows are padded to NPAD (pad rows: degree 1, no toggled column, s = 1) so
+// that one instantiation serves a range of orders; the walk itself runs the
+// true order's 2^(n-1) states.  Accumulation, the block reduction and the
+// self-zeroing result words are those of the exact kernel.
+#pragma once
+
+#include "exact_glynn.cuh"
+
+namespace pg {
+
+struct BinaryArgs {
+    const uint64_t *rmask;     // [NPAD] toggled-column bits of each row (group order)
+    const int32_t *deg;        // [NPAD] row degrees (pad rows 1)
+    const uint64_t *cmask;     // [n-1] rows of each toggled column (bit r = row r)
+    uint64_t even;             // rows of even degree (the only ones that can vanish)
+    uint64_t half[6];          // planes of deg_r / 2
+    int n;
+    unsigned long long *acc;   // [NL] per-word sums (exact kernel layout)
+    int *status;
+    unsigned int *ticket;
+    unsigned long long *out;
+    volatile const int *abort_flag;
+    uint64_t chunks;
+    int log_len;
+    uint64_t chunk0;
+    int threads;
+};
+
+constexpr int BIN_WARPS = 8;   // 256-thread blocks
+constexpr int BIN_QCAP = 64;   // queue entries per warp (32 pending + one step's 32)
+
+__host__ __device__ constexpr int binary_min_blocks(int NPAD) { return NPAD > 40 ? 1 : 2; }
+
+template <int W, int B>
+struct BitCounts {
+    uint32_t p[B][W];
+
+    __device__ __forceinline__ void set(const uint64_t *planes) {
+#pragma unroll
+        for (int b = 0; b < B; b++)
+#pragma unroll
+            for (int w = 0; w < W; w++) p[b][w] = (uint32_t)(planes[b] >> (32 * w));
+    }
+    // t_r -= 1 (dec) or += 1 for the rows in m: ripple through the planes
+    __device__ __forceinline__ void step(uint64_t m, bool dec) {
+        const uint32_t d = dec ? 0xffffffffu : 0u;
+#pragma unroll
+        for (int w = 0; w < W; w++) {
+            uint32_t c = (uint32_t)(m >> (32 * w));
+#pragma unroll
+            for (int b = 0; b < B; b++) {
+                const uint32_t t = (p[b][w] ^ d) & c;
+                p[b][w] ^= c;
+                c = t;
+            }
+        }
+    }
+    // true when no row count equals its half degree on an even-degree row
+    __device__ __forceinline__ bool nonzero(uint64_t even, const uint64_t *half) const {
+        uint32_t any = 0;
+#pragma unroll
+        for (int w = 0; w < W; w++) {
+            uint32_t z = (uint32_t)(even >> (32 * w));
+#pragma unroll
+            for (int b = 0; b < B; b++) z &= ~(p[b][w] ^ (uint32_t)(half[b] >> (32 * w)));
+            any |= z;
+        }
+        return any == 0;
+    }
+};
+
+// Exact term of state g (or a zero term when !live) into the columns.
+template <int NPAD, int G>
+__device__ __forceinline__ void binary_term(const uint64_t *rm, const int32_t *deg, uint64_t g,
+                                            bool live, uint64_t *col, int64_t &colt, bool first) {
+    const uint64_t gm = g ^ (g >> 1);
+    int32_t s[NPAD];
+#pragma unroll
+    for (int r = 0; r < NPAD; r++) s[r] = deg[r] - 2 * __popcll(rm[r] & gm);
+    if (!live) s[0] = 0;
+    exact_term_col<NPAD, G, 0>(s, col, colt, (uint32_t)(g & 1), first);
+}
+
+template <int NPAD, int G, int B>
+__global__ void __launch_bounds__(256, binary_min_blocks(NPAD))
+binary_glynn_kernel(BinaryArgs a) {
+    constexpr int W = NPAD > 32 ? 2 : 1;
+    using S = ExactShape<NPAD, G>;
+    constexpr int NL = S::NL, NR = S::NR, LOGU = 2, U = 1 << LOGU;
+    constexpr int FOLD = 1 << EXACT_LOGU;   // terms the 64-bit columns hold between folds
+    __shared__ uint64_t s_rm[NPAD];
+    __shared__ int32_t s_deg[NPAD];
+    __shared__ uint64_t s_cm[64];
+    __shared__ uint64_t s_q[BIN_WARPS][BIN_QCAP];
+    for (int i = threadIdx.x; i < NPAD; i += blockDim.x) {
+        s_rm[i] = a.rmask[i];
+        s_deg[i] = a.deg[i];
+    }
+    for (int i = threadIdx.x; i < a.n - 1; i += blockDim.x) s_cm[i] = a.cmask[i];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t below = (1u << lane) - 1u;
+    uint64_t *q = s_q[warp];
+
+    uint32_t acc[NL];
+#pragma unroll
+    for (int l = 0; l < NL; l++) acc[l] = 0;
+    uint64_t col[NR > 1 ? NR - 1 : 1];
+    int64_t colt = 0;
+    int terms = 0;       // terms in the columns since the last fold (warp-uniform)
+    int qn = 0;          // queued states (warp-uniform)
+
+    // one contiguous, balanced range of chunks per thread; the walk loop
+    // runs the warp's largest count so ballots always see all 32 lanes
+    const uint64_t T = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t c_begin = a.chunk0 + tid * a.chunks / T;
+    const uint64_t c_end = a.chunk0 + (tid + 1) * a.chunks / T;
+    const uint64_t nch = c_end - c_begin;
+    const uint64_t kmax = a.chunks / T + 1;
+    BitCounts<W, B> cnt;
+    {
+        // counts at the first state: t_r = deg_r - popc(row_r & gray(start))
+        const uint64_t start = c_begin << a.log_len;
+        const uint64_t gs = start ^ (start >> 1);
+        uint64_t planes[B];
+#pragma unroll
+        for (int b = 0; b < B; b++) planes[b] = 0;
+        for (int r = 0; r < NPAD; r++) {
+            const uint32_t t = (uint32_t)(s_deg[r] - __popcll(s_rm[r] & gs));
+#pragma unroll
+            for (int b = 0; b < B; b++) planes[b] |= (uint64_t)((t >> b) & 1u) << r;
+        }
+        cnt.set(planes);
+    }
+    const uint32_t Q = (1u << a.log_len) >> LOGU;
+    const uint64_t poll = a.log_len >= 16 ? 0 : (1ull << (16 - a.log_len)) - 1;
+    const uint64_t cm0 = s_cm[0], cm1 = a.n - 1 > 1 ? s_cm[1] : 0;
+    bool aborted = false;
+
+    auto evaluate = [&](bool flush) {
+        __syncwarp();
+        const bool live = lane < qn;
+        binary_term<NPAD, G>(s_rm, s_deg, live ? q[lane] : 0, live, col, colt, terms == 0);
+        if (++terms == FOLD) {
+            FoldCols<NR, NL>::apply(acc, col, colt);
+            terms = 0;
+        }
+        __syncwarp();
+        if (!flush) {
+            if (lane + 32 < qn) q[lane] = q[lane + 32];
+            qn -= 32;
+        }
+        __syncwarp();
+    };
+
+    for (uint64_t k = 0; k < kmax; k++) {
+        if ((k & poll) == 0 && __any_sync(0xffffffffu, *a.abort_flag != 0)) {
+            aborted = true;
+            break;
+        }
+        const bool act = k < nch;
+        const uint64_t c = c_begin + k;
+        const uint32_t hib = (uint32_t)(c & 1) << a.log_len;
+        for (uint32_t qq = 0; qq < Q; qq++) {
+            const uint32_t g32 = (qq << LOGU) | hib;
+#pragma unroll
+            for (int r = 0; r < U; r++) {
+                bool step = act;
+                uint64_t m;
+                bool dec;
+                if (r != 0) {
+                    const int j = exact_ctz_small(r);
+                    m = j == 0 ? cm0 : cm1;
+                    dec = (j + 1 < LOGU) ? ((r >> (j + 1)) & 1) == 0 : ((g32 >> LOGU) & 1) == 0;
+                } else if (qq != 0) {
+                    const int j = __ffs(qq) - 1 + LOGU;
+                    m = s_cm[j];
+                    dec = ((g32 >> (j + 1)) & 1) == 0;
+                } else {
+                    // chunk boundary (lanes may differ here); the first
+                    // state of the thread's range is the initial one
+                    step = act && k != 0;
+                    const int jc = __ffsll((long long)c) - 1;
+                    const int j = a.log_len + jc;
+                    m = step ? s_cm[j] : 0;
+                    dec = ((c >> (jc + 1)) & 1) == 0;
+                }
+                if (step) cnt.step(m, dec);
+                const bool nz = act && cnt.nonzero(a.even, a.half);
+                const uint32_t mask = __ballot_sync(0xffffffffu, nz);
+                if (mask) {
+                    if (nz) q[qn + __popc(mask & below)] = ((c << a.log_len) | g32 | (uint32_t)r);
+                    qn += __popc(mask);
+                    if (qn >= 32) evaluate(false);
+                }
+            }
+        }
+    }
+    if (qn > 0) evaluate(true);
+    if (terms > 0) FoldCols<NR, NL>::apply(acc, col, colt);
+
+    // block reduction and result words: as the exact kernel
+    __shared__ long long red[8][NL];
+    __shared__ int any_abort;
+    if (threadIdx.x == 0) any_abort = 0;
+    __syncthreads();
+    if (aborted) any_abort = 1;
+#pragma unroll
+    for (int l = 0; l < NL; l++) {
+        long long v = (l == NL - 1) ? (long long)(int32_t)acc[l] : (long long)acc[l];
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+        if (lane == 0) red[warp][l] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < NL) {
+        long long t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w][threadIdx.x];
+        atomicAdd(a.acc + threadIdx.x, (unsigned long long)t);
+    }
+    if (threadIdx.x == 0 && any_abort) atomicExch(a.status, 1);
+    __threadfence();
+    __syncthreads();
+    __shared__ bool last;
+    if (threadIdx.x == 0) last = atomicAdd(a.ticket, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (last) {
+        if (threadIdx.x < NL) a.out[threadIdx.x] = atomicExch(a.acc + threadIdx.x, 0ull);
+        if (threadIdx.x == 0) {
+            a.out[NL] = (unsigned long long)(unsigned)atomicExch(a.status, 0);
+            atomicExch(a.ticket, 0u);
+        }
+    }
+}
+
+template <int NPAD, int G, int B>
+cudaError_t launch_binary_glynn(const BinaryArgs &args, int blocks, cudaStream_t stream) {
+    binary_glynn_kernel<NPAD, G, B><<<blocks, args.threads, 0, stream>>>(args);
+    return cudaGetLastError();
+}
+
+template <int NPAD, int G, int B>
+int occupancy_binary_glynn() {
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, binary_glynn_kernel<NPAD, G, B>, 256,
+                                                      0) != cudaSuccess)
+        return 1;
+    return nb < 1 ? 1 : nb;
+}
+
+// Compiled shapes (binary_inst_*.cu): NPAD in {32, 40, 48}, G in {5, 6, 7,
+// 8, 10}, B in {3, 4, 5, 6}.  Orders below BINARY_MIN_N use the exact
+// kernel (they finish in microseconds either way).  EXACT_BINARY=0 sends
+// every 0/1 matrix to the exact kernel (for comparisons).
+constexpr int BINARY_MIN_N = 24;
+#ifndef EXACT_BINARY
+#define EXACT_BINARY 1
+#endif
+int binary_npad(int n);
+bool binary_compiled(int NPAD, int G, int B);
+cudaError_t launch_binary_any(int NPAD, int G, int B, const BinaryArgs &args, int blocks,
+                              cudaStream_t stream);
+int occupancy_binary_any(int NPAD, int G, int B);
+
+}  // namespace pg

@@ -358,6 +358,16 @@ constexpr int EXACT_MAX_G = 10;
 
 // Largest compiled float-row count for (N, G), 0 when none (exact_frows.cu).
 int exact_frows_max(int N, int G);
+// Orders each row group of `order` (n rows, groups of G) by increasing bound
+// and checks that its first exact_float_rows(n, G, FR, g) rows qualify as
+// float rows (bounds below 2^24, product below 2^22); on success rewrites
+// `order` (same group membership) and returns true (pg_exact.cu).
+bool exact_frows_arrange(const int64_t *A, int n, int G, int FR, int *order);
+__host__ __device__ inline uint32_t exact_float_bits(float f) {
+    union { float f; uint32_t u; } v;
+    v.f = f;
+    return v.u;
+}
 cudaError_t launch_exact_frows(int N, int G, int FR, const ExactArgs &args, int blocks,
                                cudaStream_t stream);
 int occupancy_exact_frows(int N, int G, int FR);

@@ -2,6 +2,7 @@
 // launch, and the carry of per-word sums into per(A) = S / 2^(n-1).
 #include "pg_internal.h"
 #include "exact_glynn.cuh"
+#include "binary_glynn.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -150,7 +151,9 @@ void exact_launch_shape(int log_states, int occ, int sm_count, uint64_t *blocks,
 // FP32 product, converted by the 1.5 * 2^23 add).  Reorders `order` in
 // place (group membership is unchanged) and returns true when every group
 // qualifies.
-static bool frows_arrange(const int64_t *A, int n, int G, int FR, std::vector<int> *order) {
+bool exact_frows_arrange(const int64_t *A, int n, int G, int FR, int *order_io) {
+    std::vector<int> ord(order_io, order_io + n);
+    std::vector<int> *order = &ord;
     if (FR <= 0) return false;
     std::vector<uint64_t> B(n);
     for (int i = 0; i < n; i++) {
@@ -174,7 +177,7 @@ static bool frows_arrange(const int64_t *A, int n, int G, int FR, std::vector<in
         }
         if (prod >= ((unsigned __int128)1 << 22)) return false;
     }
-    *order = o;
+    std::copy(o.begin(), o.end(), order_io);
     return true;
 }
 
@@ -188,6 +191,10 @@ static uint32_t float_bits(int64_t v) {
 struct ExactPlan {
     int n = 0, G = 0, NG = 0, NL = 0, need_bits = 0;
     int fr = 0;                  // float rows per group (0: integer rows)
+    // bit-sliced 0/1 kernel (binary_glynn.cuh): planes B > 0, padded rows
+    int planes = 0, npad = 0;
+    uint64_t even = 0, half[6] = {0, 0, 0, 0, 0, 0};
+    size_t off_deg = 0, off_cm = 0;
     ChunkPlan chunks{};
     uint64_t chunk0 = 0;
     uint64_t blocks = 0;
@@ -202,7 +209,89 @@ struct ExactPlan {
     volatile int *abort_dev = nullptr;
 };
 
+// The bit-sliced kernel for a 0/1 matrix of order BINARY_MIN_N..48: rows
+// padded to NPAD (degree 1, no columns), grouped by degree like the exact
+// kernel; the last column keeps the fixed sign.  False when the matrix is not
+// 0/1 or no compiled shape fits (the exact kernel then runs).
+static bool plan_build_binary(const int64_t *A, int n, ExactPlan *P) {
+    if (!EXACT_BINARY || n < BINARY_MIN_N || n > 48) return false;
+    for (size_t i = 0; i < (size_t)n * n; i++)
+        if (A[i] != 0 && A[i] != 1) return false;
+    const int NPAD = binary_npad(n);
+    std::vector<uint64_t> deg(NPAD, 1);
+    int maxdeg = 0;
+    for (int i = 0; i < n; i++) {
+        uint64_t d = 0;
+        for (int j = 0; j < n; j++) d += (uint64_t)A[(size_t)i * n + j];
+        deg[i] = d;
+        maxdeg = std::max(maxdeg, (int)d);
+    }
+    int B = 3;
+    while ((1 << B) <= maxdeg) B++;
+    if (B > 6) return false;
+    std::vector<int> order(NPAD);
+    int G = 0;
+    for (int g : {10, 8, 7, 6, 5}) {
+        if (!binary_compiled(NPAD, g, B)) continue;
+        if (exact_group_rows(deg.data(), NPAD, g, order.data())) { G = g; break; }
+    }
+    if (!G) return false;
+    P->planes = B;
+    P->npad = NPAD;
+    P->G = G;
+    P->NG = (NPAD + G - 1) / G;
+    P->NL = P->NG + (NPAD > 32 ? 2 : 1);
+    P->off_deg = align_up((size_t)NPAD * 8, 16);
+    P->off_cm = align_up(P->off_deg + (size_t)NPAD * 4, 256);
+    P->off_acc = align_up(P->off_cm + 64 * 8, 256);
+    P->image.assign(P->off_acc, 0);
+    uint64_t *rm = (uint64_t *)P->image.data();
+    int32_t *dg = (int32_t *)(P->image.data() + P->off_deg);
+    uint64_t *cm = (uint64_t *)(P->image.data() + P->off_cm);
+    P->even = 0;
+    for (int b = 0; b < 6; b++) P->half[b] = 0;
+    for (int i = 0; i < NPAD; i++) {
+        const int row = order[i];
+        dg[i] = (int32_t)deg[row];
+        uint64_t m = 0;
+        if (row < n)
+            for (int j = 0; j < n - 1; j++)
+                if (A[(size_t)row * n + j]) {
+                    m |= 1ull << j;
+                    cm[j] |= 1ull << i;
+                }
+        rm[i] = m;
+        if (deg[row] % 2 == 0) {
+            P->even |= 1ull << i;
+            for (int b = 0; b < B; b++)
+                if (((deg[row] / 2) >> b) & 1) P->half[b] |= 1ull << i;
+        }
+    }
+    return true;
+}
+
 static int plan_build(const int64_t *A, int n, ExactPlan *P) {
+    if (plan_build_binary(A, n, P)) {
+        DeviceInfo dev;
+        int st = device_info(&dev);
+        if (st != PG_OK) return st;
+        st = abort_flag_device(&P->abort_dev);
+        if (st != PG_OK) return st;
+        P->n = n;
+        P->need_bits = bound_bits(A, n) + 2;
+        P->off_status = align_up(P->off_acc + (size_t)P->NL * 8, 256);   // status, ticket at +8
+        P->off_out = align_up(P->off_status + 16, 256);
+        P->total = align_up(P->off_out + (size_t)(P->NL + 1) * 8, 256);
+        P->image.resize(P->total, 0);
+        const int occ = occupancy_binary_any(P->npad, P->G, P->planes);
+        uint64_t blocks = 0;
+        int log_len = 0;
+        exact_launch_shape(n - 1, occ, dev.sm_count, &blocks, &P->threads, &log_len);
+        P->chunks.log_len = log_len;
+        P->chunks.chunks = 1ull << (n - 1 - log_len);
+        P->blocks = blocks;
+        return PG_OK;
+    }
     std::vector<int> order;
     const int G = choose_group(A, n, &order);
     if (!G) return fail(PG_EOVERFLOW, "row-sum bound exceeds the exact engine's fixed widths");
@@ -213,7 +302,7 @@ static int plan_build(const int64_t *A, int n, ExactPlan *P) {
     if (st != PG_OK) return st;
     const int N = n, NCOL = n - 1, NP = (n + 3) & ~3;
     const int fr_max = exact_frows_max(n, G);
-    P->fr = frows_arrange(A, n, G, fr_max, &order) ? fr_max : 0;
+    P->fr = exact_frows_arrange(A, n, G, fr_max, order.data()) ? fr_max : 0;
     P->n = n;
     P->G = G;
     P->NG = (N + G - 1) / G;
@@ -265,6 +354,26 @@ static int plan_upload(ExactPlan *P) {
 
 // One launch (async on `stream`): a single kernel, no memset.
 static int plan_launch(ExactPlan *P, cudaStream_t stream) {
+    if (P->planes) {
+        BinaryArgs b;
+        b.rmask = (const uint64_t *)P->dev;
+        b.deg = (const int32_t *)(P->dev + P->off_deg);
+        b.cmask = (const uint64_t *)(P->dev + P->off_cm);
+        b.even = P->even;
+        for (int i = 0; i < 6; i++) b.half[i] = P->half[i];
+        b.n = P->n;
+        b.acc = (unsigned long long *)(P->dev + P->off_acc);
+        b.status = (int *)(P->dev + P->off_status);
+        b.ticket = (unsigned int *)(P->dev + P->off_status + 8);
+        b.out = (unsigned long long *)(P->dev + P->off_out);
+        b.abort_flag = P->abort_dev;
+        b.chunks = P->chunks.chunks;
+        b.log_len = P->chunks.log_len;
+        b.chunk0 = P->chunk0;
+        b.threads = P->threads;
+        PG_CUDA(launch_binary_any(P->npad, P->G, P->planes, b, (int)P->blocks, stream));
+        return PG_OK;
+    }
     ExactArgs args;
     args.tab = (const int32_t *)P->dev;
     args.init = (const int32_t *)(P->dev + align_up((size_t)(P->n - 1) * 2 * ((P->n + 3) & ~3) * 4, 256));
@@ -459,6 +568,10 @@ int pg_exact_plan_info(const pg_exact_plan *plan, int *group, int *words,
 
 int pg_exact_plan_float_rows(const pg_exact_plan *plan) {
     return plan ? plan->p.fr : 0;
+}
+
+int pg_exact_plan_bit_planes(const pg_exact_plan *plan) {
+    return plan ? plan->p.planes : 0;
 }
 
 void pg_exact_plan_destroy(pg_exact_plan *plan) {

@@ -49,7 +49,7 @@ struct F64Args {
 
 static constexpr int F64_M = 4;                 // low gradient columns per chunk
 
-template <int N>
+template <int N, bool GRAD>
 __global__ void __launch_bounds__(128) glynn_f64_kernel(F64Args a) {
     constexpr int LEV = N <= 2 ? 1 : N <= 4 ? 2 : N <= 8 ? 3 : N <= 16 ? 4 : 5;
     constexpr int M = (N - 1) < F64_M ? (N - 1) : F64_M;
@@ -118,19 +118,20 @@ __global__ void __launch_bounds__(128) glynn_f64_kernel(F64Args a) {
                     const df d = tab[wib][j][lane];
                     if (live) s = df_add(s, sub ? df_neg(d) : d);
                 }
-                // butterfly: T = prod_l s_l, E = prod_{l != lane} s_l
+                // butterfly: T = prod_l s_l, E = prod_{l != lane} s_l (the
+                // all-but-self products only when the gradient is wanted)
                 df T = s, E = df{1.f, 0.f};
 #pragma unroll
                 for (int lv = 0; lv < LEV; lv++) {
                     const df o = df_shfl_xor(T, 1 << lv);
-                    E = df_mul(E, o);
+                    if (GRAD) E = df_mul(E, o);
                     T = df_mul(T, o);
                 }
                 const bool odd = g & 1;                // Glynn sign (-1)^g
                 const df term = odd ? df_neg(T) : T;
                 fblk = df_add(fblk, term);
                 fabs_blk += fabsf(T.hi);
-                if (a.want_grad) {
+                if (GRAD) {
                     const df w = odd ? df_neg(E) : E;
                     gabs_blk += fabsf(E.hi);
                     W = df_add(W, w);
@@ -144,7 +145,7 @@ __global__ void __launch_bounds__(128) glynn_f64_kernel(F64Args a) {
                     }
                 }
             }
-            if (a.want_grad) {
+            if (GRAD) {
                 const uint64_t gc = c0 ^ (c0 >> 1);
 #pragma unroll
                 for (int j = 0; j < N; j++) {
@@ -162,7 +163,7 @@ __global__ void __launch_bounds__(128) glynn_f64_kernel(F64Args a) {
         kahan(fsum, fcomp, df_to(fblk));
         fabs_sum += (double)fabs_blk;
         gabs += (double)gabs_blk;
-        if (a.want_grad && live) {
+        if (GRAD && live) {
 #pragma unroll
             for (int j = 0; j < N; j++) {
                 double sm = slot[4 + lane * N + j], cp = slot[4 + N * N + lane * N + j];
@@ -243,7 +244,10 @@ __global__ void glynn_f64_reduce(F64Reduce r) {
 template <int N>
 static cudaError_t launch_f64(const F64Args &a, cudaStream_t s) {
     const long warps = (long)a.batch << a.log_w;
-    glynn_f64_kernel<N><<<(unsigned)((warps + 3) / 4), 128, 0, s>>>(a);
+    if (a.want_grad)
+        glynn_f64_kernel<N, true><<<(unsigned)((warps + 3) / 4), 128, 0, s>>>(a);
+    else
+        glynn_f64_kernel<N, false><<<(unsigned)((warps + 3) / 4), 128, 0, s>>>(a);
     return cudaGetLastError();
 }
 

@@ -77,6 +77,7 @@ SIGNATURES = {
     "pg_exact_plan_info": ([ctypes.c_void_p, _c_intp, _c_intp, _c_u64p, _c_u64p, _c_u64p], ctypes.c_int),
     "pg_exact_plan_destroy": ([ctypes.c_void_p], None),
     "pg_exact_plan_float_rows": ([ctypes.c_void_p], ctypes.c_int),
+    "pg_exact_plan_bit_planes": ([ctypes.c_void_p], ctypes.c_int),
     "pg_probe_int_throughput": ([ctypes.c_int, ctypes.c_int, _c_f64p], ctypes.c_int),
     "pg_batch_plan_create": ([_c_i64p, _c_i64p, _c_i32p, ctypes.c_int, ctypes.c_void_p,
                               ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
@@ -354,6 +355,7 @@ class ExactPlan:
         self.group, self.words, self.states = g.value, w.value, st.value
         self.imul_per_state, self.imad_wide_per_state = imul.value, wide.value
         self.float_rows = int(load().pg_exact_plan_float_rows(h))
+        self.bit_planes = int(load().pg_exact_plan_bit_planes(h))
 
     def launch(self, stream: int | None = None) -> None:
         check(load().pg_exact_plan_launch(self._h, ctypes.c_void_p(stream or 0)))
