@@ -224,9 +224,11 @@ int pg_exact_plan_info(const pg_exact_plan *plan, int *group, int *words,
  * G - FR as 32-bit IMULs.  Splits pg_exact_plan_info's multiply count by
  * pipe for the roofline (no reference counterpart). */
 int pg_exact_plan_float_rows(const pg_exact_plan *plan);
-/* Bit planes of the plan's 0/1 kernel (orders 24..48 with 0/1 entries run
- * the bit-sliced walk with zero-row skipping and exact evaluation of the
- * surviving states); 0 when the general exact kernel runs.  The binary
+/* Offset planes of the plan's 0/1 kernel (0/1 matrices of orders 24..48
+ * whose sampled share of states without a zero row is at most 1/4 run a
+ * bit-sliced walk over the even-degree rows' offsets from half their degree,
+ * modulo 2^K, with exact evaluation of the surviving states); 0 when the
+ * general exact kernel runs.  The binary
  * counterpart of rivin-perm's binary_glynn_mont32 / binary_glynn_ratio_kernel
  * (perm_binary_omp.c:236-347, perm_binary_cuda.cu:111-205), which it
  * replaces on the binary_permanent path with an exact result. */

@@ -72,6 +72,12 @@ __host__ __device__ constexpr bool batch_frows_compiled(int N, int G) {
     return (N == 20 || N == 24 || N == 28) && G == 4;
 }
 constexpr int BATCH_FROWS = 3;
+// 1: a matrix whose rows fit groups of 5 still takes groups of 4 with float
+// rows when they qualify (two FMULs and one IMUL per group of 4 instead of
+// four IMULs per group of 5).
+#ifndef BATCH_FROWS_FIRST
+#define BATCH_FROWS_FIRST 1
+#endif
 __host__ __device__ constexpr int batch_frows_order(int n) {
     return n >= 20 && n <= 28 ? (n + 3) & ~3 : 0;
 }
@@ -272,19 +278,18 @@ int pg_batch_plan_create(const int64_t *A, const int64_t *offsets, const int32_t
         }
         P.bound_bits[m] = bits;
         std::vector<int> order;
-        const int G = n < 2 || n > BATCH_MAX_N ? 0 : batch_group(a, n, &order);
+        int G = n < 2 || n > BATCH_MAX_N ? 0 : batch_group(a, n, &order);
         if (!G) {
             P.ext_index[m] = (int)P.external.size();
             P.external.emplace_back(a, a + (size_t)n * n);
             continue;
         }
         P.in_kernel[m] = 1;
-        P.groups[m] = (uint8_t)G;
         // float rows at the padded order K: a bound-only K x K image whose
         // extra rows have bound 1 picks the grouping and the float rows
         int K = n, FR = 0;
         const int KF = batch_frows_order(n);
-        if (G == 4 && batch_frows_compiled(KF, 4)) {
+        if ((G == 4 || (BATCH_FROWS_FIRST && G == 5)) && batch_frows_compiled(KF, 4)) {
             std::vector<int64_t> img((size_t)KF * KF, 0);
             for (int i = 0; i < KF; i++)
                 for (int j = 0; j < KF; j++)
@@ -300,9 +305,11 @@ int pg_batch_plan_create(const int64_t *A, const int64_t *offsets, const int32_t
                 exact_frows_arrange(img.data(), KF, 4, BATCH_FROWS, ko.data())) {
                 K = KF;
                 FR = BATCH_FROWS;
+                G = 4;
                 order = ko;
             }
         }
+        P.groups[m] = (uint8_t)G;
         P.frows[m] = (uint8_t)FR;
         P.korder[m] = (uint8_t)K;
         const int NP = (K + 3) & ~3;

@@ -1,20 +1,23 @@
-// Exact Glynn kernel for 0/1 matrices: bit-sliced row counts, zero-row
-// skipping and warp-compacted exact evaluation.
+// Exact Glynn kernel for 0/1 matrices: bit-sliced zero-row tracking and
+// warp-compacted exact evaluation of the states that survive it.
 //
 // For a 0/1 matrix the Glynn row sum of state d is s_r = deg_r - 2 m_r,
 // where m_r counts the row's ones in columns whose sign is minus.  A term
-// is zero as soon as one row sum is zero (an even-degree row with
-// m_r = deg_r / 2), which for the benchmark matrices is most states
+// is zero as soon as one row sum is zero, which needs an even degree and
+// m_r = deg_r / 2; for the benchmark matrices that is most states
 // (40 x 40 Bernoulli(1/2): ~92 %; the 4x4x5 grid: ~99.9 %).  The reference
 // keeps int16 row sums, a zero counter and a ratio-updated product mod p
 // for every state (perm_binary_omp.c:236-347, perm_binary_cuda.cu:111-205);
-// this kernel instead keeps the counts t_r = deg_r - m_r bit-sliced: plane
-// b holds bit b of every row's count, one bit per row (two 32-bit words for
-// up to 64 rows).  A Gray step adds or subtracts 1 in the rows of the
-// toggled column: a ripple carry through the planes, two three-input
-// logic operations per plane and word.  The zero test compares the planes
-// with those of deg_r / 2 on the even-degree rows: one more per plane and
-// word.  Nothing is multiplied on the walk.
+// this kernel multiplies nothing on the walk.  It tracks only the
+// even-degree rows (odd rows never vanish), each by the offset
+// u_r = t_r - deg_r / 2 (t_r = ones in plus columns) modulo 2^K, where
+// 2^K > deg_r / 2 so that u_r = 0 exactly when s_r = 0.  The offsets are
+// bit-sliced: plane b holds bit b of every tracked row's offset, one bit per
+// row (one 32-bit word for up to 32 tracked rows, two for up to 64).  A Gray
+// step adds or subtracts 1 in the tracked rows of the toggled column: a
+// ripple through the K planes, two logic operations per plane and word.
+// A state has a zero row exactly when some tracked row has all K plane bits
+// clear: one OR chain per word.
 //
 // States with no zero row are appended to a per-warp queue in shared memory
 // (a ballot gives each lane its slot).  Whenever 32 are queued, every lane
@@ -37,9 +40,10 @@ namespace pg {
 struct BinaryArgs {
     const uint64_t *rmask;     // [NPAD] toggled-column bits of each row (group order)
     const int32_t *deg;        // [NPAD] row degrees (pad rows 1)
-    const uint64_t *cmask;     // [n-1] rows of each toggled column (bit r = row r)
-    uint64_t even;             // rows of even degree (the only ones that can vanish)
-    uint64_t half[6];          // planes of deg_r / 2
+    const uint64_t *cmask;     // [n-1] tracked rows of each toggled column (bit e)
+    const uint64_t *trmask;    // [ntracked] toggled-column bits of each tracked row
+    const int32_t *toff;       // [ntracked] deg_r - deg_r / 2 (offset of the all-plus state)
+    int ntracked;              // even-degree rows, <= 32 W
     int n;
     unsigned long long *acc;   // [NL] per-word sums (exact kernel layout)
     int *status;
@@ -57,41 +61,36 @@ constexpr int BIN_QCAP = 64;   // queue entries per warp (32 pending + one step'
 
 __host__ __device__ constexpr int binary_min_blocks(int NPAD) { return NPAD > 40 ? 1 : 2; }
 
-template <int W, int B>
-struct BitCounts {
-    uint32_t p[B][W];
+template <int W, int K>
+struct ZeroTracker {
+    uint32_t p[K][W];
+    uint32_t valid[W];        // tracked rows present in each word
 
-    __device__ __forceinline__ void set(const uint64_t *planes) {
-#pragma unroll
-        for (int b = 0; b < B; b++)
-#pragma unroll
-            for (int w = 0; w < W; w++) p[b][w] = (uint32_t)(planes[b] >> (32 * w));
-    }
-    // t_r -= 1 (dec) or += 1 for the rows in m: ripple through the planes
+    // t -= 1 (dec) or += 1 for the tracked rows in m, modulo 2^K
     __device__ __forceinline__ void step(uint64_t m, bool dec) {
         const uint32_t d = dec ? 0xffffffffu : 0u;
 #pragma unroll
         for (int w = 0; w < W; w++) {
             uint32_t c = (uint32_t)(m >> (32 * w));
 #pragma unroll
-            for (int b = 0; b < B; b++) {
+            for (int b = 0; b < K; b++) {
                 const uint32_t t = (p[b][w] ^ d) & c;
                 p[b][w] ^= c;
                 c = t;
             }
         }
     }
-    // true when no row count equals its half degree on an even-degree row
-    __device__ __forceinline__ bool nonzero(uint64_t even, const uint64_t *half) const {
-        uint32_t any = 0;
+    // true when no tracked row has offset 0 (no zero row sum)
+    __device__ __forceinline__ bool nonzero() const {
+        uint32_t zero = 0;
 #pragma unroll
         for (int w = 0; w < W; w++) {
-            uint32_t z = (uint32_t)(even >> (32 * w));
+            uint32_t any = p[0][w];
 #pragma unroll
-            for (int b = 0; b < B; b++) z &= ~(p[b][w] ^ (uint32_t)(half[b] >> (32 * w)));
-            any |= z;
+            for (int b = 1; b < K; b++) any |= p[b][w];
+            zero |= valid[w] & ~any;
         }
-        return any == 0;
+        return zero == 0;
     }
 };
 
@@ -107,10 +106,9 @@ __device__ __forceinline__ void binary_term(const uint64_t *rm, const int32_t *d
     exact_term_col<NPAD, G, 0>(s, col, colt, (uint32_t)(g & 1), first);
 }
 
-template <int NPAD, int G, int B>
+template <int NPAD, int G, int K, int W>
 __global__ void __launch_bounds__(256, binary_min_blocks(NPAD))
 binary_glynn_kernel(BinaryArgs a) {
-    constexpr int W = NPAD > 32 ? 2 : 1;
     using S = ExactShape<NPAD, G>;
     constexpr int NL = S::NL, NR = S::NR, LOGU = 2, U = 1 << LOGU;
     constexpr int FOLD = 1 << EXACT_LOGU;   // terms the 64-bit columns hold between folds
@@ -144,20 +142,26 @@ binary_glynn_kernel(BinaryArgs a) {
     const uint64_t c_end = a.chunk0 + (tid + 1) * a.chunks / T;
     const uint64_t nch = c_end - c_begin;
     const uint64_t kmax = a.chunks / T + 1;
-    BitCounts<W, B> cnt;
+    ZeroTracker<W, K> zt;
     {
-        // counts at the first state: t_r = deg_r - popc(row_r & gray(start))
+        // offsets at the first state: u_e = toff_e - popc(row_e & gray(start)) mod 2^K
         const uint64_t start = c_begin << a.log_len;
         const uint64_t gs = start ^ (start >> 1);
-        uint64_t planes[B];
+        uint64_t planes[K];
 #pragma unroll
-        for (int b = 0; b < B; b++) planes[b] = 0;
-        for (int r = 0; r < NPAD; r++) {
-            const uint32_t t = (uint32_t)(s_deg[r] - __popcll(s_rm[r] & gs));
+        for (int b = 0; b < K; b++) planes[b] = 0;
+        for (int e = 0; e < a.ntracked; e++) {
+            const uint32_t u = (uint32_t)(a.toff[e] - __popcll(a.trmask[e] & gs));
 #pragma unroll
-            for (int b = 0; b < B; b++) planes[b] |= (uint64_t)((t >> b) & 1u) << r;
+            for (int b = 0; b < K; b++) planes[b] |= (uint64_t)((u >> b) & 1u) << e;
         }
-        cnt.set(planes);
+        const uint64_t valid = a.ntracked >= 64 ? ~0ull : (1ull << a.ntracked) - 1;
+#pragma unroll
+        for (int w = 0; w < W; w++) {
+            zt.valid[w] = (uint32_t)(valid >> (32 * w));
+#pragma unroll
+            for (int b = 0; b < K; b++) zt.p[b][w] = (uint32_t)(planes[b] >> (32 * w));
+        }
     }
     const uint32_t Q = (1u << a.log_len) >> LOGU;
     const uint64_t poll = a.log_len >= 16 ? 0 : (1ull << (16 - a.log_len)) - 1;
@@ -212,8 +216,8 @@ binary_glynn_kernel(BinaryArgs a) {
                     m = step ? s_cm[j] : 0;
                     dec = ((c >> (jc + 1)) & 1) == 0;
                 }
-                if (step) cnt.step(m, dec);
-                const bool nz = act && cnt.nonzero(a.even, a.half);
+                if (step) zt.step(m, dec);
+                const bool nz = act && zt.nonzero();
                 const uint32_t mask = __ballot_sync(0xffffffffu, nz);
                 if (mask) {
                     if (nz) q[qn + __popc(mask & below)] = ((c << a.log_len) | g32 | (uint32_t)r);
@@ -260,33 +264,36 @@ binary_glynn_kernel(BinaryArgs a) {
     }
 }
 
-template <int NPAD, int G, int B>
+template <int NPAD, int G, int K, int W>
 cudaError_t launch_binary_glynn(const BinaryArgs &args, int blocks, cudaStream_t stream) {
-    binary_glynn_kernel<NPAD, G, B><<<blocks, args.threads, 0, stream>>>(args);
+    binary_glynn_kernel<NPAD, G, K, W><<<blocks, args.threads, 0, stream>>>(args);
     return cudaGetLastError();
 }
 
-template <int NPAD, int G, int B>
+template <int NPAD, int G, int K, int W>
 int occupancy_binary_glynn() {
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, binary_glynn_kernel<NPAD, G, B>, 256,
-                                                      0) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, binary_glynn_kernel<NPAD, G, K, W>,
+                                                      256, 0) != cudaSuccess)
         return 1;
     return nb < 1 ? 1 : nb;
 }
 
 // Compiled shapes (binary_inst_*.cu): NPAD in {32, 40, 48}, G in {5, 6, 7,
-// 8, 10}, B in {3, 4, 5, 6}.  Orders below BINARY_MIN_N use the exact
-// kernel (they finish in microseconds either way).  EXACT_BINARY=0 sends
-// every 0/1 matrix to the exact kernel (for comparisons).
+// 8, 10}, K in {2, 3, 4, 5} offset planes, W = 1 tracking word (2 for
+// NPAD 40 and 48 with more than 32 even-degree rows).  Orders below
+// BINARY_MIN_N, and matrices whose sampled share of states without a zero
+// row exceeds BINARY_MAX_SURVIVORS, use the exact kernel.  EXACT_BINARY=0
+// sends every 0/1 matrix to the exact kernel (for comparisons).
 constexpr int BINARY_MIN_N = 24;
+constexpr double BINARY_MAX_SURVIVORS = 0.25;
 #ifndef EXACT_BINARY
 #define EXACT_BINARY 1
 #endif
 int binary_npad(int n);
-bool binary_compiled(int NPAD, int G, int B);
-cudaError_t launch_binary_any(int NPAD, int G, int B, const BinaryArgs &args, int blocks,
+bool binary_compiled(int NPAD, int G, int K, int W);
+cudaError_t launch_binary_any(int NPAD, int G, int K, int W, const BinaryArgs &args, int blocks,
                               cudaStream_t stream);
-int occupancy_binary_any(int NPAD, int G, int B);
+int occupancy_binary_any(int NPAD, int G, int K, int W);
 
 }  // namespace pg

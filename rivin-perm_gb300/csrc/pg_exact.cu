@@ -191,10 +191,10 @@ static uint32_t float_bits(int64_t v) {
 struct ExactPlan {
     int n = 0, G = 0, NG = 0, NL = 0, need_bits = 0;
     int fr = 0;                  // float rows per group (0: integer rows)
-    // bit-sliced 0/1 kernel (binary_glynn.cuh): planes B > 0, padded rows
-    int planes = 0, npad = 0;
-    uint64_t even = 0, half[6] = {0, 0, 0, 0, 0, 0};
-    size_t off_deg = 0, off_cm = 0;
+    // bit-sliced 0/1 kernel (binary_glynn.cuh): offset planes K > 0,
+    // tracking words W, tracked (even-degree) rows, padded rows
+    int planes = 0, words_tracked = 0, ntracked = 0, npad = 0;
+    size_t off_deg = 0, off_cm = 0, off_trm = 0, off_toff = 0;
     ChunkPlan chunks{};
     uint64_t chunk0 = 0;
     uint64_t blocks = 0;
@@ -209,63 +209,87 @@ struct ExactPlan {
     volatile int *abort_dev = nullptr;
 };
 
-// The bit-sliced kernel for a 0/1 matrix of order BINARY_MIN_N..48: rows
-// padded to NPAD (degree 1, no columns), grouped by degree like the exact
-// kernel; the last column keeps the fixed sign.  False when the matrix is not
-// 0/1 or no compiled shape fits (the exact kernel then runs).
+// The bit-sliced kernel for a 0/1 matrix of order BINARY_MIN_N..48: the
+// even-degree rows are tracked for zero row sums, rows are padded to NPAD
+// (degree 1, no columns) and grouped by degree like the exact kernel; the
+// last column keeps the fixed sign.  The share of states with no zero row
+// is estimated from 1024 sampled states: above BINARY_MAX_SURVIVORS the
+// exact evaluations would cost more than the general kernel, which then
+// runs (as it does when the matrix is not 0/1 or no compiled shape fits).
 static bool plan_build_binary(const int64_t *A, int n, ExactPlan *P) {
     if (!EXACT_BINARY || n < BINARY_MIN_N || n > 48) return false;
     for (size_t i = 0; i < (size_t)n * n; i++)
         if (A[i] != 0 && A[i] != 1) return false;
     const int NPAD = binary_npad(n);
-    std::vector<uint64_t> deg(NPAD, 1);
-    int maxdeg = 0;
+    std::vector<uint64_t> deg(NPAD, 1), rows(NPAD, 0);
+    std::vector<int> tracked;
+    int maxh = 0;
     for (int i = 0; i < n; i++) {
-        uint64_t d = 0;
-        for (int j = 0; j < n; j++) d += (uint64_t)A[(size_t)i * n + j];
+        uint64_t d = 0, m = 0;
+        for (int j = 0; j < n; j++) {
+            d += (uint64_t)A[(size_t)i * n + j];
+            if (j < n - 1 && A[(size_t)i * n + j]) m |= 1ull << j;
+        }
         deg[i] = d;
-        maxdeg = std::max(maxdeg, (int)d);
+        rows[i] = m;
+        if (d % 2 == 0) {
+            tracked.push_back(i);
+            maxh = std::max(maxh, (int)(d / 2));
+        }
     }
-    int B = 3;
-    while ((1 << B) <= maxdeg) B++;
-    if (B > 6) return false;
+    if (tracked.empty()) return false;          // no row can vanish: every state counts
+    int K = 2;
+    while ((1 << K) <= maxh) K++;
+    const int W = tracked.size() > 32 ? 2 : 1;
+    // sampled share of states with no zero row (fixed LCG, Gray words)
+    uint64_t x = 0x9e3779b97f4a7c15ull;
+    int survive = 0;
+    const int samples = 1024;
+    const uint64_t state_mask = (1ull << (n - 1)) - 1;
+    for (int t = 0; t < samples; t++) {
+        x = x * 6364136223846793005ull + 1442695040888963407ull;
+        const uint64_t g = (x >> 11) & state_mask, gm = g ^ (g >> 1);
+        bool zero = false;
+        for (int r : tracked)
+            if (2 * (uint64_t)__builtin_popcountll(rows[r] & gm) == deg[r]) { zero = true; break; }
+        survive += !zero;
+    }
+    if (survive > BINARY_MAX_SURVIVORS * samples) return false;
     std::vector<int> order(NPAD);
     int G = 0;
     for (int g : {10, 8, 7, 6, 5}) {
-        if (!binary_compiled(NPAD, g, B)) continue;
+        if (!binary_compiled(NPAD, g, K, W)) continue;
         if (exact_group_rows(deg.data(), NPAD, g, order.data())) { G = g; break; }
     }
     if (!G) return false;
-    P->planes = B;
+    P->planes = K;
+    P->words_tracked = W;
+    P->ntracked = (int)tracked.size();
     P->npad = NPAD;
     P->G = G;
     P->NG = (NPAD + G - 1) / G;
     P->NL = P->NG + (NPAD > 32 ? 2 : 1);
     P->off_deg = align_up((size_t)NPAD * 8, 16);
     P->off_cm = align_up(P->off_deg + (size_t)NPAD * 4, 256);
-    P->off_acc = align_up(P->off_cm + 64 * 8, 256);
+    P->off_trm = align_up(P->off_cm + 64 * 8, 256);
+    P->off_toff = align_up(P->off_trm + 64 * 8, 16);
+    P->off_acc = align_up(P->off_toff + 64 * 4, 256);
     P->image.assign(P->off_acc, 0);
     uint64_t *rm = (uint64_t *)P->image.data();
     int32_t *dg = (int32_t *)(P->image.data() + P->off_deg);
     uint64_t *cm = (uint64_t *)(P->image.data() + P->off_cm);
-    P->even = 0;
-    for (int b = 0; b < 6; b++) P->half[b] = 0;
+    uint64_t *trm = (uint64_t *)(P->image.data() + P->off_trm);
+    int32_t *toff = (int32_t *)(P->image.data() + P->off_toff);
     for (int i = 0; i < NPAD; i++) {
-        const int row = order[i];
-        dg[i] = (int32_t)deg[row];
-        uint64_t m = 0;
-        if (row < n)
-            for (int j = 0; j < n - 1; j++)
-                if (A[(size_t)row * n + j]) {
-                    m |= 1ull << j;
-                    cm[j] |= 1ull << i;
-                }
-        rm[i] = m;
-        if (deg[row] % 2 == 0) {
-            P->even |= 1ull << i;
-            for (int b = 0; b < B; b++)
-                if (((deg[row] / 2) >> b) & 1) P->half[b] |= 1ull << i;
-        }
+        rm[i] = rows[order[i]];
+        dg[i] = (int32_t)deg[order[i]];
+    }
+    for (size_t e = 0; e < tracked.size(); e++) {
+        const int r = tracked[e];
+        trm[e] = rows[r];
+        toff[e] = (int32_t)(deg[r] / 2);        // u = deg/2 - (ones in minus columns)
+        for (int j = 0; j < n - 1; j++)
+            if ((rows[r] >> j) & 1) cm[j] |= 1ull << e;
     }
     return true;
 }
@@ -283,7 +307,7 @@ static int plan_build(const int64_t *A, int n, ExactPlan *P) {
         P->off_out = align_up(P->off_status + 16, 256);
         P->total = align_up(P->off_out + (size_t)(P->NL + 1) * 8, 256);
         P->image.resize(P->total, 0);
-        const int occ = occupancy_binary_any(P->npad, P->G, P->planes);
+        const int occ = occupancy_binary_any(P->npad, P->G, P->planes, P->words_tracked);
         uint64_t blocks = 0;
         int log_len = 0;
         exact_launch_shape(n - 1, occ, dev.sm_count, &blocks, &P->threads, &log_len);
@@ -359,8 +383,9 @@ static int plan_launch(ExactPlan *P, cudaStream_t stream) {
         b.rmask = (const uint64_t *)P->dev;
         b.deg = (const int32_t *)(P->dev + P->off_deg);
         b.cmask = (const uint64_t *)(P->dev + P->off_cm);
-        b.even = P->even;
-        for (int i = 0; i < 6; i++) b.half[i] = P->half[i];
+        b.trmask = (const uint64_t *)(P->dev + P->off_trm);
+        b.toff = (const int32_t *)(P->dev + P->off_toff);
+        b.ntracked = P->ntracked;
         b.n = P->n;
         b.acc = (unsigned long long *)(P->dev + P->off_acc);
         b.status = (int *)(P->dev + P->off_status);
@@ -371,7 +396,8 @@ static int plan_launch(ExactPlan *P, cudaStream_t stream) {
         b.log_len = P->chunks.log_len;
         b.chunk0 = P->chunk0;
         b.threads = P->threads;
-        PG_CUDA(launch_binary_any(P->npad, P->G, P->planes, b, (int)P->blocks, stream));
+        PG_CUDA(launch_binary_any(P->npad, P->G, P->planes, P->words_tracked, b,
+                                  (int)P->blocks, stream));
         return PG_OK;
     }
     ExactArgs args;

@@ -1,12 +1,14 @@
 """GPU parity of the bit-sliced 0/1 kernel (binary_glynn.cuh) that the exact
-engine runs for 0/1 matrices of order 24..48.
+engine runs for 0/1 matrices of order 24..48 with few surviving states.
 
 Doubling one row of a 0/1 matrix doubles its permanent and sends it to the
 general exact kernel (entries no longer 0/1), which is pinned to the
 reference's exact values; the 0/1 kernel's result must equal half of it for
-every order, density, bit-plane count (maximum degree 7, 15, 31, 63) and
+every order, density, number of offset planes K (half-degrees up to 3, 7,
+15, 31), tracking width (up to 32 and up to 64 even-degree rows) and
 row-group size the host can pick.  Zero rows, permutation matrices and
-all-ones blocks check the zero-row test at its edges.
+all-ones blocks check the edges of the zero-row test and the host's choice
+between the two kernels.
 """
 
 import math
@@ -27,45 +29,49 @@ def _via_general_kernel(lib, a):
     return _exact(lib, b) // 2
 
 
+def _planes(lib, a):
+    plan = lib.ExactPlan(a)
+    k = plan.bit_planes
+    plan.close()
+    return k
+
+
+def _even_rows(n, degree, seed):
+    rng = np.random.default_rng(seed)
+    a = np.zeros((n, n), dtype=np.int64)
+    for i in range(n):
+        a[i, rng.choice(n, size=degree, replace=False)] = 1
+    return a
+
+
 @pytest.mark.parametrize("n,density", [(24, 0.5), (25, 0.3), (28, 0.5), (30, 0.15), (31, 0.7),
                                        (32, 0.5), (33, 0.5), (36, 0.2), (37, 0.5)])
 def test_binary_kernel_matches_general_kernel(lib, n, density):
     rng = np.random.default_rng(int(1000 * density) + n)
     a = (rng.random((n, n)) < density).astype(np.int64)
-    plan = lib.ExactPlan(a)
-    assert plan.bit_planes >= 3
-    plan.close()
+    if density == 0.5:
+        assert _planes(lib, a) >= 2          # dense random 0/1: the 0/1 kernel runs
     assert _exact(lib, a) == _via_general_kernel(lib, a)
 
 
-@pytest.mark.parametrize("maxdeg", [7, 15, 31])
-def test_every_bit_plane_count(lib, maxdeg):
-    # rows of degree up to maxdeg (3, 4, 5 planes) at order 30
-    n = 30
-    rng = np.random.default_rng(maxdeg)
-    a = np.zeros((n, n), dtype=np.int64)
-    for i in range(n):
-        d = int(rng.integers(1, maxdeg + 1)) if i else maxdeg
-        a[i, rng.choice(n, size=min(d, n), replace=False)] = 1
-    plan = lib.ExactPlan(a)
-    want_planes = max(3, int(a.sum(1).max()).bit_length())
-    assert plan.bit_planes == want_planes
-    plan.close()
+@pytest.mark.parametrize("degree,planes", [(6, 2), (14, 3), (22, 4)])
+def test_every_offset_plane_count(lib, degree, planes):
+    # all rows of one even degree at order 30: K = smallest with 2^K > degree/2
+    a = _even_rows(30, degree, degree)
+    assert _planes(lib, a) == planes
     assert _exact(lib, a) == _via_general_kernel(lib, a)
 
 
-def test_six_planes_dense_order_40(lib):
-    # degrees near 36 need 6 planes; a 2^22-state window keeps it short,
-    # against the general kernel's window on the row-doubled matrix
+def test_five_planes_and_two_tracking_words_order_44(lib):
+    # 44 even rows of degree 36 (K = 5, more than 32 tracked rows: two
+    # words); 2^22-state windows keep it short, against the general
+    # kernel's windows on the row-doubled matrix
     from permgpu import shard
-    n = 40
-    a = (np.random.default_rng(40).random((n, n)) < 0.9).astype(np.int64)
-    plan = lib.ExactPlan(a)
-    assert plan.bit_planes == 6
-    plan.close()
+    a = _even_rows(44, 36, 44)
+    assert _planes(lib, a) == 5
     b = a.copy()
     b[0] *= 2
-    for lo in (0, 1 << 30, (1 << 39) - (1 << 22)):
+    for lo in (0, 1 << 30, (1 << 43) - (1 << 22)):
         v = shard.words_value(shard.exact_partial_words(a, lo, lo + (1 << 22)))
         w = shard.words_value(shard.exact_partial_words(b, lo, lo + (1 << 22)))
         assert 2 * v == w
@@ -77,11 +83,14 @@ def test_zero_rows_permutations_and_ones(lib):
     a = (rng.random((n, n)) < 0.5).astype(np.int64)
     a[5] = 0                                             # a zero row
     assert _exact(lib, a) == 0
-    p = np.eye(n, dtype=np.int64)[rng.permutation(n)]    # a permutation matrix
+    p = np.eye(n, dtype=np.int64)[rng.permutation(n)]    # odd degrees: general kernel
+    assert _planes(lib, p) == 0
     assert _exact(lib, p) == 1
-    j = np.ones((n, n), dtype=np.int64)                  # every row even: n!
+    j = np.ones((n, n), dtype=np.int64)                  # equal rows: most states survive
+    assert _planes(lib, j) == 0
     assert _exact(lib, j) == math.factorial(n)
-    j25 = np.ones((25, 25), dtype=np.int64)              # odd degrees: no zero row
-    assert _exact(lib, j25) == math.factorial(25)
-    blocks = np.kron(np.eye(2, dtype=np.int64), np.ones((13, 13), dtype=np.int64))
-    assert _exact(lib, blocks) == math.factorial(13) ** 2
+    blocks = np.kron(np.eye(2, dtype=np.int64), np.ones((14, 14), dtype=np.int64))
+    assert _exact(lib, blocks) == math.factorial(14) ** 2
+    sparse = _even_rows(40, 4, 4)                        # K = 2, nearly every state zero
+    assert _planes(lib, sparse) == 2
+    assert _exact(lib, sparse) == _via_general_kernel(lib, sparse)
