@@ -49,6 +49,7 @@ struct BinaryArgs {
     int *status;
     unsigned int *ticket;
     unsigned long long *out;
+    unsigned long long *part;  // [gridDim][NL] per-block slots (exact_epilogue), or nullptr
     volatile const int *abort_flag;
     uint64_t chunks;
     int log_len;
@@ -134,18 +135,23 @@ binary_glynn_kernel(BinaryArgs a) {
     int terms = 0;       // terms in the columns since the last fold (warp-uniform)
     int qn = 0;          // queued states (warp-uniform)
 
-    // one contiguous, balanced range of chunks per thread; the walk loop
-    // runs the warp's largest count so ballots always see all 32 lanes
+    // Chunks are dealt round-robin: thread t walks chunks t, t + T, t + 2T,
+    // ... of the window, so every thread (and every SM) samples the whole
+    // walk.  The share of surviving states varies strongly along the walk
+    // (it depends on the signs of the high columns), and contiguous ranges
+    // per thread left some SMs with most of the exact evaluations.  Each
+    // chunk starts from a closed-form tracker state.  Lanes of a warp take
+    // consecutive chunks, so the step's column is warp-uniform, and the walk
+    // loop runs the same count on every lane so ballots see all 32.
     const uint64_t T = (uint64_t)gridDim.x * blockDim.x;
     const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const uint64_t c_begin = a.chunk0 + tid * a.chunks / T;
-    const uint64_t c_end = a.chunk0 + (tid + 1) * a.chunks / T;
-    const uint64_t nch = c_end - c_begin;
-    const uint64_t kmax = a.chunks / T + 1;
+    const uint64_t kmax = (a.chunks + T - 1) / T;
+    const uint64_t valid = a.ntracked >= 64 ? ~0ull : (1ull << a.ntracked) - 1;
     ZeroTracker<W, K> zt;
-    {
-        // offsets at the first state: u_e = toff_e - popc(row_e & gray(start)) mod 2^K
-        const uint64_t start = c_begin << a.log_len;
+#pragma unroll
+    for (int w = 0; w < W; w++) zt.valid[w] = (uint32_t)(valid >> (32 * w));
+    // offsets at state `start`: u_e = toff_e - popc(row_e & gray(start)) mod 2^K
+    auto init_tracker = [&](uint64_t start) {
         const uint64_t gs = start ^ (start >> 1);
         uint64_t planes[K];
 #pragma unroll
@@ -155,14 +161,11 @@ binary_glynn_kernel(BinaryArgs a) {
 #pragma unroll
             for (int b = 0; b < K; b++) planes[b] |= (uint64_t)((u >> b) & 1u) << e;
         }
-        const uint64_t valid = a.ntracked >= 64 ? ~0ull : (1ull << a.ntracked) - 1;
 #pragma unroll
-        for (int w = 0; w < W; w++) {
-            zt.valid[w] = (uint32_t)(valid >> (32 * w));
+        for (int w = 0; w < W; w++)
 #pragma unroll
             for (int b = 0; b < K; b++) zt.p[b][w] = (uint32_t)(planes[b] >> (32 * w));
-        }
-    }
+    };
     const uint32_t Q = (1u << a.log_len) >> LOGU;
     const uint64_t poll = a.log_len >= 16 ? 0 : (1ull << (16 - a.log_len)) - 1;
     const uint64_t cm0 = s_cm[0], cm1 = a.n - 1 > 1 ? s_cm[1] : 0;
@@ -189,16 +192,19 @@ binary_glynn_kernel(BinaryArgs a) {
             aborted = true;
             break;
         }
-        const bool act = k < nch;
-        const uint64_t c = c_begin + k;
+        const uint64_t ci = k * T + tid;
+        const bool act = ci < a.chunks;
+        const uint64_t c = a.chunk0 + ci;
+        if (act) init_tracker(c << a.log_len);
         const uint32_t hib = (uint32_t)(c & 1) << a.log_len;
         for (uint32_t qq = 0; qq < Q; qq++) {
             const uint32_t g32 = (qq << LOGU) | hib;
 #pragma unroll
             for (int r = 0; r < U; r++) {
-                bool step = act;
-                uint64_t m;
-                bool dec;
+                // the chunk's first state is the initialised one
+                const bool step = act && (r != 0 || qq != 0);
+                uint64_t m = 0;
+                bool dec = false;
                 if (r != 0) {
                     const int j = exact_ctz_small(r);
                     m = j == 0 ? cm0 : cm1;
@@ -207,14 +213,6 @@ binary_glynn_kernel(BinaryArgs a) {
                     const int j = __ffs(qq) - 1 + LOGU;
                     m = s_cm[j];
                     dec = ((g32 >> (j + 1)) & 1) == 0;
-                } else {
-                    // chunk boundary (lanes may differ here); the first
-                    // state of the thread's range is the initial one
-                    step = act && k != 0;
-                    const int jc = __ffsll((long long)c) - 1;
-                    const int j = a.log_len + jc;
-                    m = step ? s_cm[j] : 0;
-                    dec = ((c >> (jc + 1)) & 1) == 0;
                 }
                 if (step) zt.step(m, dec);
                 const bool nz = act && zt.nonzero();
@@ -244,24 +242,7 @@ binary_glynn_kernel(BinaryArgs a) {
         if (lane == 0) red[warp][l] = v;
     }
     __syncthreads();
-    if (threadIdx.x < NL) {
-        long long t = 0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w][threadIdx.x];
-        atomicAdd(a.acc + threadIdx.x, (unsigned long long)t);
-    }
-    if (threadIdx.x == 0 && any_abort) atomicExch(a.status, 1);
-    __threadfence();
-    __syncthreads();
-    __shared__ bool last;
-    if (threadIdx.x == 0) last = atomicAdd(a.ticket, 1u) == gridDim.x - 1;
-    __syncthreads();
-    if (last) {
-        if (threadIdx.x < NL) a.out[threadIdx.x] = atomicExch(a.acc + threadIdx.x, 0ull);
-        if (threadIdx.x == 0) {
-            a.out[NL] = (unsigned long long)(unsigned)atomicExch(a.status, 0);
-            atomicExch(a.ticket, 0u);
-        }
-    }
+    exact_epilogue<NL>(red, any_abort, a.acc, a.part, a.status, a.ticket, a.out);
 }
 
 template <int NPAD, int G, int K, int W>

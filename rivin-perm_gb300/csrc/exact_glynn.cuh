@@ -214,12 +214,15 @@ struct ExactArgs {
     const int32_t *init;       // [NP] row sums of the all-plus state
     unsigned long long *acc;   // [NL] per-word sums (two's complement, zeroed)
     int *status;
-    // Launch ticket and result words: the last block to finish copies acc
-    // and the status into out[0..NL] and re-zeroes acc, status and ticket,
-    // so back-to-back launches of one plan need no memset (zero all four
-    // once before the first launch).
+    // Launch ticket and result words: the last block to finish copies the
+    // totals and the status into out[0..NL] and re-zeroes acc, status and
+    // ticket, so back-to-back launches of one plan need no memset (zero all
+    // four once before the first launch).
     unsigned int *ticket;
     unsigned long long *out;   // [NL + 1]: the words, then the status
+    // Per-block word slots [gridDim][NL] (written in full by every launch),
+    // or nullptr: blocks then add their words into acc with atomics.
+    unsigned long long *part = nullptr;
     volatile const int *abort_flag;
     uint64_t chunks;           // chunks to walk: [chunk0, chunk0 + chunks)
     int log_len;               // >= LOGU, <= 30
@@ -253,6 +256,57 @@ __host__ __device__ constexpr int exact_min_blocks(int N) {
            : (65536 / (256 * (N + 64)));
 }
 
+// Epilogue of the exact kernels, after the warps' word sums are in red[][]
+// and the block has synchronised.  Each block's words go to its own slot of
+// part[] (no two blocks touch one address, so the fence below waits for
+// nothing but the block's own stores), or with part == nullptr are added
+// into acc[] with atomics.  The block that finishes last (ticket after a
+// fence) sums the slots, or takes acc, into out[0..NL), moves the status to
+// out[NL] and re-arms acc, status and ticket for the next launch.
+template <int NL>
+__device__ __forceinline__ void exact_epilogue(long long (*red)[NL], bool any_abort,
+                                               unsigned long long *acc, unsigned long long *part,
+                                               int *status, unsigned int *ticket,
+                                               unsigned long long *out) {
+    const int nwarps = (int)(blockDim.x >> 5), lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x < NL) {
+        long long t = 0;
+        for (int w = 0; w < nwarps; w++) t += red[w][threadIdx.x];
+        if (part) part[(size_t)blockIdx.x * NL + threadIdx.x] = (unsigned long long)t;
+        else atomicAdd(acc + threadIdx.x, (unsigned long long)t);
+    }
+    if (threadIdx.x == 0 && any_abort) atomicExch(status, 1);
+    __threadfence();
+    __syncthreads();
+    __shared__ bool last;
+    if (threadIdx.x == 0) last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    if (part) {
+#pragma unroll 1
+        for (int l = 0; l < NL; l++) {
+            long long t = 0;
+            for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x)
+                t += (long long)__ldcg(part + (size_t)b * NL + l);
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) t += __shfl_down_sync(0xffffffffu, t, off);
+            if (lane == 0) red[warp][l] = t;
+        }
+        __syncthreads();
+        if (threadIdx.x < NL) {
+            long long t = 0;
+            for (int w = 0; w < nwarps; w++) t += red[w][threadIdx.x];
+            out[threadIdx.x] = (unsigned long long)t;
+        }
+    } else if (threadIdx.x < NL) {
+        out[threadIdx.x] = atomicExch(acc + threadIdx.x, 0ull);
+    }
+    if (threadIdx.x == 0) {
+        out[NL] = (unsigned long long)(unsigned)atomicExch(status, 0);
+        atomicExch(ticket, 0u);
+    }
+}
+
 template <int N, int G, int FR = 0>
 __global__ void __launch_bounds__(256, exact_min_blocks(N))
 exact_glynn_kernel(ExactArgs a) {
@@ -260,8 +314,10 @@ exact_glynn_kernel(ExactArgs a) {
     constexpr int NP = S::NP, NL = S::NL, NCOL = N - 1;
     extern __shared__ int4 esmem[];
     int32_t *tab = reinterpret_cast<int32_t *>(esmem);
+    int32_t *sinit = tab + NCOL * 2 * NP;     // the all-plus row sums, after the table
     for (int i = threadIdx.x; i < NCOL * 2 * NP / 4; i += blockDim.x)
         esmem[i] = reinterpret_cast<const int4 *>(a.tab)[i];
+    for (int i = threadIdx.x; i < NP; i += blockDim.x) sinit[i] = a.init[i];
     __syncthreads();
 
     uint32_t acc[NL];
@@ -276,7 +332,7 @@ exact_glynn_kernel(ExactArgs a) {
     bool aborted = false;
     if (c_begin < c_end) {
         int32_t s[N];
-        exact_init<N, G, FR>(tab, a.init, s, c_begin << a.log_len);
+        exact_init<N, G, FR>(tab, sinit, s, c_begin << a.log_len);
         aborted = !exact_walk<N, G, FR>(tab, s, acc, c_begin, c_end, a.log_len, a.abort_flag);
     }
 
@@ -296,33 +352,14 @@ exact_glynn_kernel(ExactArgs a) {
         if (lane == 0) red[warp][l] = v;
     }
     __syncthreads();
-    if (threadIdx.x < NL) {
-        long long t = 0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w][threadIdx.x];
-        atomicAdd(a.acc + threadIdx.x, (unsigned long long)t);
-    }
-    if (threadIdx.x == 0 && any_abort) atomicExch(a.status, 1);
-    // the block that finishes last moves the totals out and re-arms the
-    // accumulators (the fence orders this block's atomics before its ticket)
-    __threadfence();
-    __syncthreads();
-    __shared__ bool last;
-    if (threadIdx.x == 0) last = atomicAdd(a.ticket, 1u) == gridDim.x - 1;
-    __syncthreads();
-    if (last) {
-        if (threadIdx.x < NL) a.out[threadIdx.x] = atomicExch(a.acc + threadIdx.x, 0ull);
-        if (threadIdx.x == 0) {
-            a.out[NL] = (unsigned long long)(unsigned)atomicExch(a.status, 0);
-            atomicExch(a.ticket, 0u);
-        }
-    }
+    exact_epilogue<NL>(red, any_abort, a.acc, a.part, a.status, a.ticket, a.out);
 }
 
 template <int N, int G, int FR = 0>
 cudaError_t launch_exact_glynn(const ExactArgs &args, int blocks,
                                cudaStream_t stream) {
     constexpr int NP = ExactShape<N, G>::NP;
-    const size_t smem = (size_t)(N - 1) * 2 * NP * sizeof(int32_t);
+    const size_t smem = ((size_t)(N - 1) * 2 * NP + NP) * sizeof(int32_t);
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(
             exact_glynn_kernel<N, G, FR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -336,7 +373,7 @@ cudaError_t launch_exact_glynn(const ExactArgs &args, int blocks,
 template <int N, int G, int FR = 0>
 int occupancy_exact_glynn() {
     constexpr int NP = ExactShape<N, G>::NP;
-    const size_t smem = (size_t)(N - 1) * 2 * NP * sizeof(int32_t);
+    const size_t smem = ((size_t)(N - 1) * 2 * NP + NP) * sizeof(int32_t);
     if (smem > 48 * 1024)
         cudaFuncSetAttribute(exact_glynn_kernel<N, G, FR>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -199,7 +199,7 @@ struct ExactPlan {
     uint64_t chunk0 = 0;
     uint64_t blocks = 0;
     int threads = 256;
-    size_t off_acc = 0, off_status = 0, off_out = 0, total = 0;
+    size_t off_acc = 0, off_status = 0, off_out = 0, off_part = 0, total = 0;
     std::vector<char> image;     // host image of [tab | init | acc | status]
     // device side (owned by a plan object, or borrowed from a workspace)
     char *dev = nullptr;
@@ -294,6 +294,13 @@ static bool plan_build_binary(const int64_t *A, int n, ExactPlan *P) {
     return true;
 }
 
+// Per-block word slots after the result words (the kernels' epilogue).
+static void add_block_slots(ExactPlan *P) {
+    P->off_part = P->total;
+    P->total = align_up(P->off_part + (size_t)P->blocks * P->NL * 8, 256);
+    P->image.resize(P->total, 0);
+}
+
 static int plan_build(const int64_t *A, int n, ExactPlan *P) {
     if (plan_build_binary(A, n, P)) {
         DeviceInfo dev;
@@ -311,9 +318,14 @@ static int plan_build(const int64_t *A, int n, ExactPlan *P) {
         uint64_t blocks = 0;
         int log_len = 0;
         exact_launch_shape(n - 1, occ, dev.sm_count, &blocks, &P->threads, &log_len);
+        // chunks of 2^10 states (each starts from a closed-form tracker
+        // state) while every thread still gets 16 of them round-robin
+        const uint64_t T = blocks * (uint64_t)P->threads;
+        while (log_len < 10 && ((1ull << (n - 1)) >> (log_len + 1)) >= 16 * T) log_len++;
         P->chunks.log_len = log_len;
         P->chunks.chunks = 1ull << (n - 1 - log_len);
         P->blocks = blocks;
+        add_block_slots(P);
         return PG_OK;
     }
     std::vector<int> order;
@@ -363,6 +375,7 @@ static int plan_build(const int64_t *A, int n, ExactPlan *P) {
     P->chunks.log_len = log_len;
     P->chunks.chunks = 1ull << (log_states - log_len);
     P->blocks = blocks;
+    add_block_slots(P);
     return PG_OK;
 }
 
@@ -391,6 +404,7 @@ static int plan_launch(ExactPlan *P, cudaStream_t stream) {
         b.status = (int *)(P->dev + P->off_status);
         b.ticket = (unsigned int *)(P->dev + P->off_status + 8);
         b.out = (unsigned long long *)(P->dev + P->off_out);
+        b.part = (unsigned long long *)(P->dev + P->off_part);
         b.abort_flag = P->abort_dev;
         b.chunks = P->chunks.chunks;
         b.log_len = P->chunks.log_len;
@@ -412,6 +426,7 @@ static int plan_launch(ExactPlan *P, cudaStream_t stream) {
     args.threads = P->threads;
     args.ticket = (unsigned int *)(P->dev + P->off_status + 8);
     args.out = (unsigned long long *)(P->dev + P->off_out);
+    args.part = (unsigned long long *)(P->dev + P->off_part);
     PG_CUDA(P->fr ? launch_exact_frows(P->n, P->G, P->fr, args, (int)P->blocks, stream)
                   : launch_exact_any(P->n, P->G, args, (int)P->blocks, stream));
     return PG_OK;

@@ -62,16 +62,16 @@ def test_every_offset_plane_count(lib, degree, planes):
     assert _exact(lib, a) == _via_general_kernel(lib, a)
 
 
-def test_five_planes_and_two_tracking_words_order_44(lib):
-    # 44 even rows of degree 36 (K = 5, more than 32 tracked rows: two
-    # words); 2^22-state windows keep it short, against the general
-    # kernel's windows on the row-doubled matrix
+def test_five_planes_and_two_tracking_words_order_48(lib):
+    # 48 even rows of degree 32 (K = 5, more than 32 tracked rows: two
+    # words; about 1/8 of the states survive); 2^22-state windows keep it
+    # short, against the general kernel's windows on the row-doubled matrix
     from permgpu import shard
-    a = _even_rows(44, 36, 44)
+    a = _even_rows(48, 32, 48)
     assert _planes(lib, a) == 5
     b = a.copy()
     b[0] *= 2
-    for lo in (0, 1 << 30, (1 << 43) - (1 << 22)):
+    for lo in (0, 1 << 30, (1 << 47) - (1 << 22)):
         v = shard.words_value(shard.exact_partial_words(a, lo, lo + (1 << 22)))
         w = shard.words_value(shard.exact_partial_words(b, lo, lo + (1 << 22)))
         assert 2 * v == w
