@@ -283,14 +283,20 @@ __device__ __forceinline__ void exact_epilogue(long long (*red)[NL], bool any_ab
     __syncthreads();
     if (!last) return;
     if (part) {
-#pragma unroll 1
-        for (int l = 0; l < NL; l++) {
-            long long t = 0;
-            for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x)
-                t += (long long)__ldcg(part + (size_t)b * NL + l);
+        // every word's loads in flight at once, then one shuffle tree per word
+        long long t[NL];
 #pragma unroll
-            for (int off = 16; off > 0; off >>= 1) t += __shfl_down_sync(0xffffffffu, t, off);
-            if (lane == 0) red[warp][l] = t;
+        for (int l = 0; l < NL; l++) t[l] = 0;
+        for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+            const unsigned long long *slot = part + (size_t)b * NL;
+#pragma unroll
+            for (int l = 0; l < NL; l++) t[l] += (long long)__ldcg(slot + l);
+        }
+#pragma unroll
+        for (int l = 0; l < NL; l++) {
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) t[l] += __shfl_down_sync(0xffffffffu, t[l], off);
+            if (lane == 0) red[warp][l] = t[l];
         }
         __syncthreads();
         if (threadIdx.x < NL) {

@@ -294,7 +294,12 @@ static bool plan_build_binary(const int64_t *A, int n, ExactPlan *P) {
     return true;
 }
 
-// Per-block word slots after the result words (the kernels' epilogue).
+// Per-block word slots after the result words (the kernels' epilogue);
+// EXACT_BLOCK_SLOTS=0 makes the general kernel add into the shared words
+// with atomics instead (for comparisons).
+#ifndef EXACT_BLOCK_SLOTS
+#define EXACT_BLOCK_SLOTS 1
+#endif
 static void add_block_slots(ExactPlan *P) {
     P->off_part = P->total;
     P->total = align_up(P->off_part + (size_t)P->blocks * P->NL * 8, 256);
@@ -426,7 +431,7 @@ static int plan_launch(ExactPlan *P, cudaStream_t stream) {
     args.threads = P->threads;
     args.ticket = (unsigned int *)(P->dev + P->off_status + 8);
     args.out = (unsigned long long *)(P->dev + P->off_out);
-    args.part = (unsigned long long *)(P->dev + P->off_part);
+    args.part = EXACT_BLOCK_SLOTS ? (unsigned long long *)(P->dev + P->off_part) : nullptr;
     PG_CUDA(P->fr ? launch_exact_frows(P->n, P->G, P->fr, args, (int)P->blocks, stream)
                   : launch_exact_any(P->n, P->G, args, (int)P->blocks, stream));
     return PG_OK;
