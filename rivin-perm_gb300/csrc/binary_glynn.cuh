@@ -95,10 +95,29 @@ struct ZeroTracker {
     }
 };
 
-// Exact term of state g (or a zero term when !live) into the columns.
+// Exact term of state g (or a zero term when !live) into the columns.  The
+// Gray bits of g from the split up are those of the warp's current chunk
+// group, and base[r] already holds deg_r minus twice the row's ones among
+// them, so one 32-bit popcount per row remains.
 template <int NPAD, int G>
-__device__ __forceinline__ void binary_term(const uint64_t *rm, const int32_t *deg, uint64_t g,
-                                            bool live, uint64_t *col, int64_t &colt, bool first) {
+__device__ __forceinline__ void binary_term(const uint64_t *rm, const int32_t *base, uint64_t g,
+                                            bool live, uint32_t lowmask, uint64_t *col,
+                                            int64_t &colt, bool first) {
+    const uint32_t gl = (uint32_t)(g ^ (g >> 1)) & lowmask;
+    int32_t s[NPAD];
+#pragma unroll
+    for (int r = 0; r < NPAD; r++) s[r] = base[r] - 2 * __popc((uint32_t)rm[r] & gl);
+    if (!live) s[0] = 0;
+    exact_term_col<NPAD, G, 0>(s, col, colt, (uint32_t)(g & 1), first);
+}
+
+// The same for windows whose first chunk is not a multiple of 32 (no common
+// high bits): the whole 64-bit Gray word is counted.  Kept out of line so
+// that the common path's registers stay free.
+template <int NPAD, int G>
+__device__ __noinline__ void binary_term_full(const uint64_t *rm, const int32_t *deg, uint64_t g,
+                                              bool live, uint64_t *col, int64_t &colt,
+                                              bool first) {
     const uint64_t gm = g ^ (g >> 1);
     int32_t s[NPAD];
 #pragma unroll
@@ -117,6 +136,7 @@ binary_glynn_kernel(BinaryArgs a) {
     __shared__ int32_t s_deg[NPAD];
     __shared__ uint64_t s_cm[64];
     __shared__ uint64_t s_q[BIN_WARPS][BIN_QCAP];
+    __shared__ int32_t s_base[BIN_WARPS][NPAD];
     for (int i = threadIdx.x; i < NPAD; i += blockDim.x) {
         s_rm[i] = a.rmask[i];
         s_deg[i] = a.deg[i];
@@ -171,10 +191,24 @@ binary_glynn_kernel(BinaryArgs a) {
     const uint64_t cm0 = s_cm[0], cm1 = a.n - 1 > 1 ? s_cm[1] : 0;
     bool aborted = false;
 
+    // The warp's lanes walk 32 consecutive chunks; when the window starts on
+    // a multiple of 32 chunks, Gray bits from log_len + 5 up are common to
+    // them, and the queue is emptied at the end of each chunk group so that
+    // every queued state shares the group's high bits (s_base).
+    const bool split = (a.chunk0 & 31) == 0 && a.log_len + 5 <= 31;
+    const int sb = split ? a.log_len + 5 : 0;
+    const uint32_t lowmask = split ? (1u << sb) - 1u : 0xffffffffu;
+    const int32_t *base = split ? s_base[warp] : s_deg;
+
     auto evaluate = [&](bool flush) {
         __syncwarp();
         const bool live = lane < qn;
-        binary_term<NPAD, G>(s_rm, s_deg, live ? q[lane] : 0, live, col, colt, terms == 0);
+        if (split)
+            binary_term<NPAD, G>(s_rm, base, live ? q[lane] : 0, live, lowmask, col, colt,
+                                 terms == 0);
+        else
+            binary_term_full<NPAD, G>(s_rm, s_deg, live ? q[lane] : 0, live, col, colt,
+                                      terms == 0);
         if (++terms == FOLD) {
             FoldCols<NR, NL>::apply(acc, col, colt);
             terms = 0;
@@ -196,6 +230,13 @@ binary_glynn_kernel(BinaryArgs a) {
         const bool act = ci < a.chunks;
         const uint64_t c = a.chunk0 + ci;
         if (act) init_tracker(c << a.log_len);
+        if (split) {
+            // the group's common Gray bits (the queue is empty here)
+            const uint64_t g0 = c << a.log_len;
+            const uint64_t gh = (g0 ^ (g0 >> 1)) & ~(uint64_t)lowmask;
+            for (int r = lane; r < NPAD; r += 32) s_base[warp][r] = s_deg[r] - 2 * __popcll(s_rm[r] & gh);
+            __syncwarp();
+        }
         const uint32_t hib = (uint32_t)(c & 1) << a.log_len;
         for (uint32_t qq = 0; qq < Q; qq++) {
             const uint32_t g32 = (qq << LOGU) | hib;
@@ -223,6 +264,10 @@ binary_glynn_kernel(BinaryArgs a) {
                     if (qn >= 32) evaluate(false);
                 }
             }
+        }
+        if (split && qn > 0) {      // the next group has other high bits
+            evaluate(true);
+            qn = 0;
         }
     }
     if (qn > 0) evaluate(true);
