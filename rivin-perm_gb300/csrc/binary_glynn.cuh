@@ -30,7 +30,7 @@
 // Rows are padded to NPAD (pad rows: degree 1, no toggled column, s = 1) so
 // that one instantiation serves a range of orders; the walk itself runs the
 // true order's 2^(n-1) states.  Accumulation, the block reduction and the
-// self-zeroing result words are those of the exact kernel.
+// per-block result slots are those of the exact kernel.
 #pragma once
 
 #include "exact_glynn.cuh"
@@ -44,11 +44,10 @@ struct BinaryArgs {
     const uint64_t *trmask;    // [ntracked] toggled-column bits of each tracked row
     const int32_t *toff;       // [ntracked] deg_r - deg_r / 2 (offset of the all-plus state)
     int ntracked;              // even-degree rows, <= 32 W
+    int split_ok;              // evaluate from the warp's common high Gray bits (see below)
     int n;
     unsigned long long *acc;   // [NL] per-word sums (exact kernel layout)
     int *status;
-    unsigned int *ticket;
-    unsigned long long *out;
     unsigned long long *part;  // [gridDim][NL] per-block slots (exact_epilogue), or nullptr
     volatile const int *abort_flag;
     uint64_t chunks;
@@ -194,8 +193,10 @@ binary_glynn_kernel(BinaryArgs a) {
     // The warp's lanes walk 32 consecutive chunks; when the window starts on
     // a multiple of 32 chunks, Gray bits from log_len + 5 up are common to
     // them, and the queue is emptied at the end of each chunk group so that
-    // every queued state shares the group's high bits (s_base).
-    const bool split = (a.chunk0 & 31) == 0 && a.log_len + 5 <= 31;
+    // every queued state shares the group's high bits (s_base).  The host
+    // turns this off when survivors are rare: the partial rounds of the
+    // per-group flush then cost more than the popcounts they save.
+    const bool split = a.split_ok && (a.chunk0 & 31) == 0 && a.log_len + 5 <= 31;
     const int sb = split ? a.log_len + 5 : 0;
     const uint32_t lowmask = split ? (1u << sb) - 1u : 0xffffffffu;
     const int32_t *base = split ? s_base[warp] : s_deg;
@@ -287,7 +288,7 @@ binary_glynn_kernel(BinaryArgs a) {
         if (lane == 0) red[warp][l] = v;
     }
     __syncthreads();
-    exact_epilogue<NL>(red, any_abort, a.acc, a.part, a.status, a.ticket, a.out);
+    exact_epilogue<NL>(red, any_abort, a.acc, a.part, a.status);
 }
 
 template <int NPAD, int G, int K, int W>

@@ -214,14 +214,9 @@ struct ExactArgs {
     const int32_t *init;       // [NP] row sums of the all-plus state
     unsigned long long *acc;   // [NL] per-word sums (two's complement, zeroed)
     int *status;
-    // Launch ticket and result words: the last block to finish copies the
-    // totals and the status into out[0..NL] and re-zeroes acc, status and
-    // ticket, so back-to-back launches of one plan need no memset (zero all
-    // four once before the first launch).
-    unsigned int *ticket;
-    unsigned long long *out;   // [NL + 1]: the words, then the status
     // Per-block word slots [gridDim][NL] (written in full by every launch),
-    // or nullptr: blocks then add their words into acc with atomics.
+    // or nullptr: blocks then add their words into acc with atomics.  The
+    // finishing kernel (exact_finish) turns either into the result words.
     unsigned long long *part = nullptr;
     volatile const int *abort_flag;
     uint64_t chunks;           // chunks to walk: [chunk0, chunk0 + chunks)
@@ -257,61 +252,32 @@ __host__ __device__ constexpr int exact_min_blocks(int N) {
 }
 
 // Epilogue of the exact kernels, after the warps' word sums are in red[][]
-// and the block has synchronised.  Each block's words go to its own slot of
-// part[] (no two blocks touch one address, so the fence below waits for
-// nothing but the block's own stores), or with part == nullptr are added
-// into acc[] with atomics.  The block that finishes last (ticket after a
-// fence) sums the slots, or takes acc, into out[0..NL), moves the status to
-// out[NL] and re-arms acc, status and ticket for the next launch.
+// and the block has synchronised: the block's words go to its own slot of
+// part[] (no two blocks touch one address), or with part == nullptr are
+// added into acc[] with atomics; an abort is recorded in *status.  Summing
+// the slots is left to a one-block kernel launched after it (exact_finish):
+// doing it in the last block to finish made the compiler lay out the walk
+// loop worse (1-3 % at orders 28..32).
 template <int NL>
 __device__ __forceinline__ void exact_epilogue(long long (*red)[NL], bool any_abort,
                                                unsigned long long *acc, unsigned long long *part,
-                                               int *status, unsigned int *ticket,
-                                               unsigned long long *out) {
-    const int nwarps = (int)(blockDim.x >> 5), lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+                                               int *status) {
     if (threadIdx.x < NL) {
         long long t = 0;
-        for (int w = 0; w < nwarps; w++) t += red[w][threadIdx.x];
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w][threadIdx.x];
         if (part) part[(size_t)blockIdx.x * NL + threadIdx.x] = (unsigned long long)t;
         else atomicAdd(acc + threadIdx.x, (unsigned long long)t);
     }
     if (threadIdx.x == 0 && any_abort) atomicExch(status, 1);
-    __threadfence();
-    __syncthreads();
-    __shared__ bool last;
-    if (threadIdx.x == 0) last = atomicAdd(ticket, 1u) == gridDim.x - 1;
-    __syncthreads();
-    if (!last) return;
-    if (part) {
-        // every word's loads in flight at once, then one shuffle tree per word
-        long long t[NL];
-#pragma unroll
-        for (int l = 0; l < NL; l++) t[l] = 0;
-        for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
-            const unsigned long long *slot = part + (size_t)b * NL;
-#pragma unroll
-            for (int l = 0; l < NL; l++) t[l] += (long long)__ldcg(slot + l);
-        }
-#pragma unroll
-        for (int l = 0; l < NL; l++) {
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) t[l] += __shfl_down_sync(0xffffffffu, t[l], off);
-            if (lane == 0) red[warp][l] = t[l];
-        }
-        __syncthreads();
-        if (threadIdx.x < NL) {
-            long long t = 0;
-            for (int w = 0; w < nwarps; w++) t += red[w][threadIdx.x];
-            out[threadIdx.x] = (unsigned long long)t;
-        }
-    } else if (threadIdx.x < NL) {
-        out[threadIdx.x] = atomicExch(acc + threadIdx.x, 0ull);
-    }
-    if (threadIdx.x == 0) {
-        out[NL] = (unsigned long long)(unsigned)atomicExch(status, 0);
-        atomicExch(ticket, 0u);
-    }
 }
+
+// Launches the finishing kernel on `stream` after an exact or 0/1 kernel of
+// `blocks` blocks: out[0..nl) = the sum of the slots (or acc, re-zeroed,
+// when part is nullptr), out[nl] = *status, then *status = 0, so the next
+// launch starts clean without a memset (pg_exact.cu).
+cudaError_t exact_finish(const unsigned long long *part, int blocks, int nl,
+                         unsigned long long *acc, int *status, unsigned long long *out,
+                         cudaStream_t stream);
 
 template <int N, int G, int FR = 0>
 __global__ void __launch_bounds__(256, exact_min_blocks(N))
@@ -320,10 +286,8 @@ exact_glynn_kernel(ExactArgs a) {
     constexpr int NP = S::NP, NL = S::NL, NCOL = N - 1;
     extern __shared__ int4 esmem[];
     int32_t *tab = reinterpret_cast<int32_t *>(esmem);
-    int32_t *sinit = tab + NCOL * 2 * NP;     // the all-plus row sums, after the table
     for (int i = threadIdx.x; i < NCOL * 2 * NP / 4; i += blockDim.x)
         esmem[i] = reinterpret_cast<const int4 *>(a.tab)[i];
-    for (int i = threadIdx.x; i < NP; i += blockDim.x) sinit[i] = a.init[i];
     __syncthreads();
 
     uint32_t acc[NL];
@@ -338,7 +302,7 @@ exact_glynn_kernel(ExactArgs a) {
     bool aborted = false;
     if (c_begin < c_end) {
         int32_t s[N];
-        exact_init<N, G, FR>(tab, sinit, s, c_begin << a.log_len);
+        exact_init<N, G, FR>(tab, a.init, s, c_begin << a.log_len);
         aborted = !exact_walk<N, G, FR>(tab, s, acc, c_begin, c_end, a.log_len, a.abort_flag);
     }
 
@@ -358,14 +322,14 @@ exact_glynn_kernel(ExactArgs a) {
         if (lane == 0) red[warp][l] = v;
     }
     __syncthreads();
-    exact_epilogue<NL>(red, any_abort, a.acc, a.part, a.status, a.ticket, a.out);
+    exact_epilogue<NL>(red, any_abort, a.acc, a.part, a.status);
 }
 
 template <int N, int G, int FR = 0>
 cudaError_t launch_exact_glynn(const ExactArgs &args, int blocks,
                                cudaStream_t stream) {
     constexpr int NP = ExactShape<N, G>::NP;
-    const size_t smem = ((size_t)(N - 1) * 2 * NP + NP) * sizeof(int32_t);
+    const size_t smem = (size_t)(N - 1) * 2 * NP * sizeof(int32_t);
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(
             exact_glynn_kernel<N, G, FR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -379,7 +343,7 @@ cudaError_t launch_exact_glynn(const ExactArgs &args, int blocks,
 template <int N, int G, int FR = 0>
 int occupancy_exact_glynn() {
     constexpr int NP = ExactShape<N, G>::NP;
-    const size_t smem = ((size_t)(N - 1) * 2 * NP + NP) * sizeof(int32_t);
+    const size_t smem = (size_t)(N - 1) * 2 * NP * sizeof(int32_t);
     if (smem > 48 * 1024)
         cudaFuncSetAttribute(exact_glynn_kernel<N, G, FR>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -193,7 +193,7 @@ struct ExactPlan {
     int fr = 0;                  // float rows per group (0: integer rows)
     // bit-sliced 0/1 kernel (binary_glynn.cuh): offset planes K > 0,
     // tracking words W, tracked (even-degree) rows, padded rows
-    int planes = 0, words_tracked = 0, ntracked = 0, npad = 0;
+    int planes = 0, words_tracked = 0, ntracked = 0, npad = 0, bin_split = 0;
     size_t off_deg = 0, off_cm = 0, off_trm = 0, off_toff = 0;
     ChunkPlan chunks{};
     uint64_t chunk0 = 0;
@@ -255,6 +255,9 @@ static bool plan_build_binary(const int64_t *A, int n, ExactPlan *P) {
         survive += !zero;
     }
     if (survive > BINARY_MAX_SURVIVORS * samples) return false;
+    // evaluation from the warp's common high bits pays from a survivor
+    // share of about 1/64 (40x40 Bernoulli(1/2): ~8 %; the grid: ~0.1 %)
+    P->bin_split = survive * 64 >= samples;
     std::vector<int> order(NPAD);
     int G = 0;
     for (int g : {10, 8, 7, 6, 5}) {
@@ -294,6 +297,48 @@ static bool plan_build_binary(const int64_t *A, int n, ExactPlan *P) {
     return true;
 }
 
+// One block sums the per-block slots of an exact or 0/1 launch into the
+// result words (or takes the atomically added words, re-zeroing them) and
+// moves the status out, re-arming it for the next launch.
+__global__ void __launch_bounds__(256) exact_finish_kernel(const unsigned long long *part,
+                                                           int blocks, int nl,
+                                                           unsigned long long *acc, int *status,
+                                                           unsigned long long *out) {
+    __shared__ long long red[8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int l = 0; l < nl; l++) {
+        long long t = 0;
+        if (part) {
+            for (int b = threadIdx.x; b < blocks; b += blockDim.x)
+                t += (long long)part[(size_t)b * nl + l];
+        } else if (threadIdx.x == 0) {
+            t = (long long)acc[l];
+            acc[l] = 0;
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) t += __shfl_down_sync(0xffffffffu, t, off);
+        if (lane == 0) red[warp] = t;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            long long v = 0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); w++) v += red[w];
+            out[l] = (unsigned long long)v;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[nl] = (unsigned long long)(unsigned)*status;
+        *status = 0;
+    }
+}
+
+cudaError_t exact_finish(const unsigned long long *part, int blocks, int nl,
+                         unsigned long long *acc, int *status, unsigned long long *out,
+                         cudaStream_t stream) {
+    exact_finish_kernel<<<1, 256, 0, stream>>>(part, blocks, nl, acc, status, out);
+    return cudaGetLastError();
+}
+
 // Per-block word slots after the result words (the kernels' epilogue);
 // EXACT_BLOCK_SLOTS=0 makes the general kernel add into the shared words
 // with atomics instead (for comparisons).
@@ -315,7 +360,7 @@ static int plan_build(const int64_t *A, int n, ExactPlan *P) {
         if (st != PG_OK) return st;
         P->n = n;
         P->need_bits = bound_bits(A, n) + 2;
-        P->off_status = align_up(P->off_acc + (size_t)P->NL * 8, 256);   // status, ticket at +8
+        P->off_status = align_up(P->off_acc + (size_t)P->NL * 8, 256);
         P->off_out = align_up(P->off_status + 16, 256);
         P->total = align_up(P->off_out + (size_t)(P->NL + 1) * 8, 256);
         P->image.resize(P->total, 0);
@@ -351,7 +396,7 @@ static int plan_build(const int64_t *A, int n, ExactPlan *P) {
     P->need_bits = bound_bits(A, n) + 2;
     const size_t off_init = align_up((size_t)NCOL * 2 * NP * 4, 256);
     P->off_acc = align_up(off_init + (size_t)NP * 4, 256);
-    P->off_status = align_up(P->off_acc + (size_t)P->NL * 8, 256);   // status, ticket at +8
+    P->off_status = align_up(P->off_acc + (size_t)P->NL * 8, 256);
     P->off_out = align_up(P->off_status + 16, 256);
     P->total = align_up(P->off_out + (size_t)(P->NL + 1) * 8, 256);
     P->image.assign(P->total, 0);
@@ -384,7 +429,7 @@ static int plan_build(const int64_t *A, int n, ExactPlan *P) {
     return PG_OK;
 }
 
-// Upload tables and zero the accumulators, status, ticket and result words
+// Upload tables and zero the accumulators, status and result words
 // (async on P->stream).  Launches re-zero what they use, so this runs once
 // per plan.
 static int plan_upload(ExactPlan *P) {
@@ -394,7 +439,8 @@ static int plan_upload(ExactPlan *P) {
     return PG_OK;
 }
 
-// One launch (async on `stream`): a single kernel, no memset.
+// One launch (async on `stream`): the kernel and its one-block finisher,
+// no memset.
 static int plan_launch(ExactPlan *P, cudaStream_t stream) {
     if (P->planes) {
         BinaryArgs b;
@@ -404,11 +450,10 @@ static int plan_launch(ExactPlan *P, cudaStream_t stream) {
         b.trmask = (const uint64_t *)(P->dev + P->off_trm);
         b.toff = (const int32_t *)(P->dev + P->off_toff);
         b.ntracked = P->ntracked;
+        b.split_ok = P->bin_split;
         b.n = P->n;
         b.acc = (unsigned long long *)(P->dev + P->off_acc);
         b.status = (int *)(P->dev + P->off_status);
-        b.ticket = (unsigned int *)(P->dev + P->off_status + 8);
-        b.out = (unsigned long long *)(P->dev + P->off_out);
         b.part = (unsigned long long *)(P->dev + P->off_part);
         b.abort_flag = P->abort_dev;
         b.chunks = P->chunks.chunks;
@@ -417,6 +462,8 @@ static int plan_launch(ExactPlan *P, cudaStream_t stream) {
         b.threads = P->threads;
         PG_CUDA(launch_binary_any(P->npad, P->G, P->planes, P->words_tracked, b,
                                   (int)P->blocks, stream));
+        PG_CUDA(exact_finish(b.part, (int)P->blocks, P->NL, b.acc, b.status,
+                             (unsigned long long *)(P->dev + P->off_out), stream));
         return PG_OK;
     }
     ExactArgs args;
@@ -429,11 +476,11 @@ static int plan_launch(ExactPlan *P, cudaStream_t stream) {
     args.log_len = P->chunks.log_len;
     args.chunk0 = P->chunk0;
     args.threads = P->threads;
-    args.ticket = (unsigned int *)(P->dev + P->off_status + 8);
-    args.out = (unsigned long long *)(P->dev + P->off_out);
     args.part = EXACT_BLOCK_SLOTS ? (unsigned long long *)(P->dev + P->off_part) : nullptr;
     PG_CUDA(P->fr ? launch_exact_frows(P->n, P->G, P->fr, args, (int)P->blocks, stream)
                   : launch_exact_any(P->n, P->G, args, (int)P->blocks, stream));
+    PG_CUDA(exact_finish(args.part, (int)P->blocks, P->NL, args.acc, args.status,
+                         (unsigned long long *)(P->dev + P->off_out), stream));
     return PG_OK;
 }
 

@@ -47,8 +47,8 @@
 
 namespace pg {
 
-// Scratch: [tables | init | acc words | status, ticket | zero word (abort
-// flag when the process has no abort word yet) | result words, status]
+// Scratch: [tables | init | acc words | status | zero word (abort flag when
+// the process has no abort word yet) | result words, status]
 static __device__ __align__(256) unsigned char g_noalloc_scratch[PG_NOALLOC_SCRATCH_BYTES];
 
 static std::mutex g_noalloc_mu;
@@ -108,7 +108,7 @@ extern "C" int pg_exact_permanent_noalloc(const int64_t *A, int n, uint32_t *out
     const int NG = (n + G - 1) / G, NL = NG + (n > 32 ? 2 : 1);
     const size_t off_init = na_align((size_t)NCOL * 2 * NP * 4);
     const size_t off_acc = na_align(off_init + (size_t)NP * 4);
-    const size_t off_status = na_align(off_acc + (size_t)NL * 8);   // status, ticket at +4
+    const size_t off_status = na_align(off_acc + (size_t)NL * 8);
     const size_t off_zero = off_status + 8;
     const size_t off_out = na_align(off_zero + 8);
     const size_t total = na_align(off_out + (size_t)(NL + 1) * 8);
@@ -140,8 +140,8 @@ extern "C" int pg_exact_permanent_noalloc(const int64_t *A, int n, uint32_t *out
     }
     cudaStream_t s = (cudaStream_t)stream;
     PG_CUDA(cudaMemcpyAsync(scratch, image, off_acc, cudaMemcpyHostToDevice, s));
-    // accumulators, status, ticket, result words and the always-zero abort
-    // word start at zero
+    // accumulators, status, result words and the always-zero abort word
+    // start at zero
     PG_CUDA(cudaMemsetAsync(scratch + off_acc, 0, total - off_acc, s));
 
     // launch shape as in the allocating path
@@ -163,9 +163,9 @@ extern "C" int pg_exact_permanent_noalloc(const int64_t *A, int n, uint32_t *out
     args.log_len = log_len;
     args.chunk0 = 0;
     args.threads = threads;
-    args.ticket = (unsigned int *)(scratch + off_status + 4);
-    args.out = (unsigned long long *)(scratch + off_out);
     PG_CUDA(launch_exact_any(n, G, args, (int)blocks, s));
+    PG_CUDA(exact_finish(nullptr, (int)blocks, NL, args.acc, args.status,
+                         (unsigned long long *)(scratch + off_out), s));
 
     long long acc[64];          // NL + 1 <= 19 for every compiled shape: words, status
     PG_CUDA(cudaMemcpyAsync(acc, scratch + off_out, (size_t)(NL + 1) * 8, cudaMemcpyDeviceToHost, s));
