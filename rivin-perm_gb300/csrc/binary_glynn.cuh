@@ -44,11 +44,10 @@ struct BinaryArgs {
     const uint64_t *trmask;    // [ntracked] toggled-column bits of each tracked row
     const int32_t *toff;       // [ntracked] deg_r - deg_r / 2 (offset of the all-plus state)
     int ntracked;              // even-degree rows, <= 32 W
-    int split_ok;              // evaluate from the warp's common high Gray bits (see below)
     int n;
     unsigned long long *acc;   // [NL] per-word sums (exact kernel layout)
     int *status;
-    unsigned long long *part;  // [gridDim][NL] per-block slots (exact_epilogue), or nullptr
+    unsigned long long *part;  // [NL][gridDim] per-block slots (exact_epilogue), or nullptr
     volatile const int *abort_flag;
     uint64_t chunks;
     int log_len;
@@ -110,11 +109,10 @@ __device__ __forceinline__ void binary_term(const uint64_t *rm, const int32_t *b
     exact_term_col<NPAD, G, 0>(s, col, colt, (uint32_t)(g & 1), first);
 }
 
-// The same for windows whose first chunk is not a multiple of 32 (no common
-// high bits): the whole 64-bit Gray word is counted.  Kept out of line so
-// that the common path's registers stay free.
+// The same without the split (rare survivors, or windows whose first chunk
+// is not a multiple of 32): the whole 64-bit Gray word is counted.
 template <int NPAD, int G>
-__device__ __noinline__ void binary_term_full(const uint64_t *rm, const int32_t *deg, uint64_t g,
+__device__ __forceinline__ void binary_term_full(const uint64_t *rm, const int32_t *deg, uint64_t g,
                                               bool live, uint64_t *col, int64_t &colt,
                                               bool first) {
     const uint64_t gm = g ^ (g >> 1);
@@ -125,7 +123,7 @@ __device__ __noinline__ void binary_term_full(const uint64_t *rm, const int32_t 
     exact_term_col<NPAD, G, 0>(s, col, colt, (uint32_t)(g & 1), first);
 }
 
-template <int NPAD, int G, int K, int W>
+template <int NPAD, int G, int K, int W, bool SPLIT>
 __global__ void __launch_bounds__(256, binary_min_blocks(NPAD))
 binary_glynn_kernel(BinaryArgs a) {
     using S = ExactShape<NPAD, G>;
@@ -196,7 +194,7 @@ binary_glynn_kernel(BinaryArgs a) {
     // every queued state shares the group's high bits (s_base).  The host
     // turns this off when survivors are rare: the partial rounds of the
     // per-group flush then cost more than the popcounts they save.
-    const bool split = a.split_ok && (a.chunk0 & 31) == 0 && a.log_len + 5 <= 31;
+    constexpr bool split = SPLIT;   // the host checks (chunk0 & 31) == 0, log_len + 5 <= 31
     const int sb = split ? a.log_len + 5 : 0;
     const uint32_t lowmask = split ? (1u << sb) - 1u : 0xffffffffu;
     const int32_t *base = split ? s_base[warp] : s_deg;
@@ -204,7 +202,7 @@ binary_glynn_kernel(BinaryArgs a) {
     auto evaluate = [&](bool flush) {
         __syncwarp();
         const bool live = lane < qn;
-        if (split)
+        if constexpr (SPLIT)
             binary_term<NPAD, G>(s_rm, base, live ? q[lane] : 0, live, lowmask, col, colt,
                                  terms == 0);
         else
@@ -292,16 +290,20 @@ binary_glynn_kernel(BinaryArgs a) {
 }
 
 template <int NPAD, int G, int K, int W>
-cudaError_t launch_binary_glynn(const BinaryArgs &args, int blocks, cudaStream_t stream) {
-    binary_glynn_kernel<NPAD, G, K, W><<<blocks, args.threads, 0, stream>>>(args);
+cudaError_t launch_binary_glynn(const BinaryArgs &args, bool split, int blocks,
+                                cudaStream_t stream) {
+    if (split)
+        binary_glynn_kernel<NPAD, G, K, W, true><<<blocks, args.threads, 0, stream>>>(args);
+    else
+        binary_glynn_kernel<NPAD, G, K, W, false><<<blocks, args.threads, 0, stream>>>(args);
     return cudaGetLastError();
 }
 
 template <int NPAD, int G, int K, int W>
 int occupancy_binary_glynn() {
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, binary_glynn_kernel<NPAD, G, K, W>,
-                                                      256, 0) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &nb, binary_glynn_kernel<NPAD, G, K, W, true>, 256, 0) != cudaSuccess)
         return 1;
     return nb < 1 ? 1 : nb;
 }
@@ -319,8 +321,8 @@ constexpr double BINARY_MAX_SURVIVORS = 0.25;
 #endif
 int binary_npad(int n);
 bool binary_compiled(int NPAD, int G, int K, int W);
-cudaError_t launch_binary_any(int NPAD, int G, int K, int W, const BinaryArgs &args, int blocks,
-                              cudaStream_t stream);
+cudaError_t launch_binary_any(int NPAD, int G, int K, int W, const BinaryArgs &args, bool split,
+                              int blocks, cudaStream_t stream);
 int occupancy_binary_any(int NPAD, int G, int K, int W);
 
 }  // namespace pg

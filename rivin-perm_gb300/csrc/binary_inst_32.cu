@@ -1,5 +1,6 @@
 // Instantiations of binary_glynn_kernel with 32 padded rows: row groups G in
-// {5, 6, 7, 8, 10}, offset planes K in {2, 3, 4, 5}, tracking words W in {1}.
+// {5, 6, 7, 8, 10}, offset planes K in {2, 3, 4, 5}, with and without the
+// split evaluation, tracking words W in {1}.
 #include "binary_glynn.cuh"
 
 namespace pg {
@@ -11,10 +12,10 @@ namespace pg {
     X(8, 2, 1) X(8, 3, 1) X(8, 4, 1) X(8, 5, 1) \
     X(10, 2, 1) X(10, 3, 1) X(10, 4, 1) X(10, 5, 1) \
 
-cudaError_t launch_binary_npad32(int G, int K, int W, const BinaryArgs &args, int blocks,
-                                  cudaStream_t stream) {
+cudaError_t launch_binary_npad32(int G, int K, int W, const BinaryArgs &args, bool split,
+                                  int blocks, cudaStream_t stream) {
 #define PG_BIN_LAUNCH(GG, KK, WW) \
-    if (G == GG && K == KK && W == WW) return launch_binary_glynn<32, GG, KK, WW>(args, blocks, stream);
+    if (G == GG && K == KK && W == WW) return launch_binary_glynn<32, GG, KK, WW>(args, split, blocks, stream);
     PG_BIN_SHAPES(PG_BIN_LAUNCH)
 #undef PG_BIN_LAUNCH
     return cudaErrorInvalidValue;
@@ -28,10 +29,10 @@ int occupancy_binary_npad32(int G, int K, int W) {
     return 1;
 }
 
-cudaError_t launch_binary_npad40(int G, int K, int W, const BinaryArgs &args, int blocks,
-                                  cudaStream_t stream);
-cudaError_t launch_binary_npad48(int G, int K, int W, const BinaryArgs &args, int blocks,
-                                  cudaStream_t stream);
+cudaError_t launch_binary_npad40(int G, int K, int W, const BinaryArgs &args, bool split,
+                                  int blocks, cudaStream_t stream);
+cudaError_t launch_binary_npad48(int G, int K, int W, const BinaryArgs &args, bool split,
+                                  int blocks, cudaStream_t stream);
 int occupancy_binary_npad40(int G, int K, int W);
 int occupancy_binary_npad48(int G, int K, int W);
 
@@ -43,12 +44,12 @@ bool binary_compiled(int NPAD, int G, int K, int W) {
     return (NPAD == 32 || NPAD == 40 || NPAD == 48) && g && K >= 2 && K <= 5 && w;
 }
 
-cudaError_t launch_binary_any(int NPAD, int G, int K, int W, const BinaryArgs &args, int blocks,
-                              cudaStream_t stream) {
+cudaError_t launch_binary_any(int NPAD, int G, int K, int W, const BinaryArgs &args, bool split,
+                              int blocks, cudaStream_t stream) {
     if (!binary_compiled(NPAD, G, K, W)) return cudaErrorInvalidValue;
-    return NPAD == 32 ? launch_binary_npad32(G, K, W, args, blocks, stream)
-         : NPAD == 40 ? launch_binary_npad40(G, K, W, args, blocks, stream)
-                      : launch_binary_npad48(G, K, W, args, blocks, stream);
+    return NPAD == 32 ? launch_binary_npad32(G, K, W, args, split, blocks, stream)
+         : NPAD == 40 ? launch_binary_npad40(G, K, W, args, split, blocks, stream)
+                      : launch_binary_npad48(G, K, W, args, split, blocks, stream);
 }
 
 int occupancy_binary_any(int NPAD, int G, int K, int W) {

@@ -214,7 +214,7 @@ struct ExactArgs {
     const int32_t *init;       // [NP] row sums of the all-plus state
     unsigned long long *acc;   // [NL] per-word sums (two's complement, zeroed)
     int *status;
-    // Per-block word slots [gridDim][NL] (written in full by every launch),
+    // Per-block word slots [NL][gridDim] (written in full by every launch),
     // or nullptr: blocks then add their words into acc with atomics.  The
     // finishing kernel (exact_finish) turns either into the result words.
     unsigned long long *part = nullptr;
@@ -265,7 +265,7 @@ __device__ __forceinline__ void exact_epilogue(long long (*red)[NL], bool any_ab
     if (threadIdx.x < NL) {
         long long t = 0;
         for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w][threadIdx.x];
-        if (part) part[(size_t)blockIdx.x * NL + threadIdx.x] = (unsigned long long)t;
+        if (part) part[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = (unsigned long long)t;
         else atomicAdd(acc + threadIdx.x, (unsigned long long)t);
     }
     if (threadIdx.x == 0 && any_abort) atomicExch(status, 1);

@@ -299,32 +299,24 @@ static bool plan_build_binary(const int64_t *A, int n, ExactPlan *P) {
 
 // One block sums the per-block slots of an exact or 0/1 launch into the
 // result words (or takes the atomically added words, re-zeroing them) and
-// moves the status out, re-arming it for the next launch.
+// moves the status out, re-arming it for the next launch.  Warp w sums words
+// w, w + 8, ...; the slots are word-major, so a warp's loads coalesce.
 __global__ void __launch_bounds__(256) exact_finish_kernel(const unsigned long long *part,
                                                            int blocks, int nl,
                                                            unsigned long long *acc, int *status,
                                                            unsigned long long *out) {
-    __shared__ long long red[8];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int l = 0; l < nl; l++) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int l = warp; l < nl; l += nw) {
         long long t = 0;
         if (part) {
-            for (int b = threadIdx.x; b < blocks; b += blockDim.x)
-                t += (long long)part[(size_t)b * nl + l];
-        } else if (threadIdx.x == 0) {
+            for (int b = lane; b < blocks; b += 32) t += (long long)part[(size_t)l * blocks + b];
+        } else if (lane == 0) {
             t = (long long)acc[l];
             acc[l] = 0;
         }
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) t += __shfl_down_sync(0xffffffffu, t, off);
-        if (lane == 0) red[warp] = t;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            long long v = 0;
-            for (int w = 0; w < (int)(blockDim.x >> 5); w++) v += red[w];
-            out[l] = (unsigned long long)v;
-        }
-        __syncthreads();
+        if (lane == 0) out[l] = (unsigned long long)t;
     }
     if (threadIdx.x == 0) {
         out[nl] = (unsigned long long)(unsigned)*status;
@@ -450,7 +442,6 @@ static int plan_launch(ExactPlan *P, cudaStream_t stream) {
         b.trmask = (const uint64_t *)(P->dev + P->off_trm);
         b.toff = (const int32_t *)(P->dev + P->off_toff);
         b.ntracked = P->ntracked;
-        b.split_ok = P->bin_split;
         b.n = P->n;
         b.acc = (unsigned long long *)(P->dev + P->off_acc);
         b.status = (int *)(P->dev + P->off_status);
@@ -460,7 +451,10 @@ static int plan_launch(ExactPlan *P, cudaStream_t stream) {
         b.log_len = P->chunks.log_len;
         b.chunk0 = P->chunk0;
         b.threads = P->threads;
-        PG_CUDA(launch_binary_any(P->npad, P->G, P->planes, P->words_tracked, b,
+        // evaluation from the warp's common high Gray bits: the window must
+        // start on a multiple of 32 chunks
+        const bool split = P->bin_split && (P->chunk0 & 31) == 0 && P->chunks.log_len + 5 <= 31;
+        PG_CUDA(launch_binary_any(P->npad, P->G, P->planes, P->words_tracked, b, split,
                                   (int)P->blocks, stream));
         PG_CUDA(exact_finish(b.part, (int)P->blocks, P->NL, b.acc, b.status,
                              (unsigned long long *)(P->dev + P->off_out), stream));
