@@ -1,9 +1,12 @@
 #!/usr/bin/env bash
 # Compile the reference's own OpenMP extensions (perm_c_omp.c,
-# perm_binary_omp.c, perm_polynomial_omp.c and perm_mod3_omp.c) from the
-# reference checkout into oracle/_ref/.  These are CPython extension modules
-# used only as the CPU checker, the golden-vector generator and the CPU
-# baseline; no reference source is copied into this repository.
+# perm_binary_omp.c, perm_polynomial_omp.c and perm_mod3_omp.c) and the
+# device code of its CUDA tools (perm_modp_cuda.cu, perm_binary_cuda.cu,
+# perm_parallel_cuda.cu) from the reference checkout into oracle/_ref/.
+# The extension modules are the CPU checker, the golden-vector generator and
+# the CPU baseline; the cubins are the reference's GPU kernels for the
+# same-GPU comparison and parity checks.  No reference source is copied into
+# this repository.
 #
 # usage: oracle/build_ref.sh REFERENCE_DIR   (the rivin-perm checkout)
 set -euo pipefail
@@ -29,5 +32,13 @@ gcc -O3 -std=c11 -fopenmp -fPIC -shared -I"$PYINC" "$REF/perm_polynomial_omp.c" 
     -o "$OUT/perm_polynomial_ext$SUFFIX" &
 gcc -O3 -fopenmp -fPIC -shared -I"$PYINC" -I"$NPINC" "$REF/perm_mod3_omp.c" \
     -o "$OUT/perm_mod3_omp$SUFFIX" &
+# the reference's CUDA kernels, device code only (cubins for sm_103a, loaded
+# through the CUDA driver API by oracle/ref_cuda.py; the host code around
+# them is restated there)
+if command -v nvcc > /dev/null; then
+  for f in perm_modp_cuda perm_binary_cuda perm_parallel_cuda; do
+    nvcc -gencode arch=compute_103a,code=sm_103a -O3 -cubin "$REF/$f.cu" -o "$OUT/$f.cubin" &
+  done
+fi
 wait
 echo "built the reference extensions into $OUT"

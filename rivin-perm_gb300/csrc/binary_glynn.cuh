@@ -48,6 +48,8 @@ struct BinaryArgs {
     unsigned long long *acc;   // [NL] per-word sums (exact kernel layout)
     int *status;
     unsigned long long *part;  // [NL][gridDim] per-block slots (exact_epilogue), or nullptr
+    unsigned long long *next;  // chunk groups taken so far beyond each warp's first; zero at
+                               // launch, re-zeroed by the finishing kernel
     volatile const int *abort_flag;
     uint64_t chunks;
     int log_len;
@@ -134,6 +136,7 @@ binary_glynn_kernel(BinaryArgs a) {
     __shared__ uint64_t s_cm[64];
     __shared__ uint64_t s_q[BIN_WARPS][BIN_QCAP];
     __shared__ int32_t s_base[BIN_WARPS][NPAD];
+    exact_allow_dependents();
     for (int i = threadIdx.x; i < NPAD; i += blockDim.x) {
         s_rm[i] = a.rmask[i];
         s_deg[i] = a.deg[i];
@@ -152,17 +155,20 @@ binary_glynn_kernel(BinaryArgs a) {
     int terms = 0;       // terms in the columns since the last fold (warp-uniform)
     int qn = 0;          // queued states (warp-uniform)
 
-    // Chunks are dealt round-robin: thread t walks chunks t, t + T, t + 2T,
-    // ... of the window, so every thread (and every SM) samples the whole
-    // walk.  The share of surviving states varies strongly along the walk
-    // (it depends on the signs of the high columns), and contiguous ranges
-    // per thread left some SMs with most of the exact evaluations.  Each
-    // chunk starts from a closed-form tracker state.  Lanes of a warp take
-    // consecutive chunks, so the step's column is warp-uniform, and the walk
-    // loop runs the same count on every lane so ballots see all 32.
+    // Chunks are dealt in groups of 32 consecutive ones, lane l of a warp
+    // taking the group's chunk l (so the step's column is warp-uniform and
+    // every lane runs the same loop count, which the ballots need).  Each
+    // warp walks its own group first and then takes the next untaken group
+    // from a counter, one atomic per 2^(log_len + 5) states.  The share of
+    // surviving states, and so the exact evaluations, varies strongly along
+    // the walk with the signs of the columns: a fixed deal (contiguous
+    // ranges, or round-robin with a stride that is a multiple of 2^12
+    // chunks, which pins twelve column signs per warp) left some SMs with
+    // 40 % more instructions than the mean.  Each chunk starts from a
+    // closed-form tracker state.
     const uint64_t T = (uint64_t)gridDim.x * blockDim.x;
     const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const uint64_t kmax = (a.chunks + T - 1) / T;
+    const uint64_t ngroups = (a.chunks + 31) >> 5;
     const uint64_t valid = a.ntracked >= 64 ? ~0ull : (1ull << a.ntracked) - 1;
     ZeroTracker<W, K> zt;
 #pragma unroll
@@ -220,12 +226,13 @@ binary_glynn_kernel(BinaryArgs a) {
         __syncwarp();
     };
 
-    for (uint64_t k = 0; k < kmax; k++) {
-        if ((k & poll) == 0 && __any_sync(0xffffffffu, *a.abort_flag != 0)) {
+    uint64_t grp = tid >> 5;              // the warp's own group first
+    for (uint64_t k = 0; grp < ngroups; k++) {
+        if (k != 0 && (k & poll) == 0 && __any_sync(0xffffffffu, *a.abort_flag != 0)) {
             aborted = true;
             break;
         }
-        const uint64_t ci = k * T + tid;
+        const uint64_t ci = (grp << 5) + lane;
         const bool act = ci < a.chunks;
         const uint64_t c = a.chunk0 + ci;
         if (act) init_tracker(c << a.log_len);
@@ -268,6 +275,9 @@ binary_glynn_kernel(BinaryArgs a) {
             evaluate(true);
             qn = 0;
         }
+        unsigned long long nx = 0;
+        if (lane == 0) nx = (T >> 5) + atomicAdd(a.next, 1ull);
+        grp = __shfl_sync(0xffffffffu, nx, 0);
     }
     if (qn > 0) evaluate(true);
     if (terms > 0) FoldCols<NR, NL>::apply(acc, col, colt);

@@ -163,10 +163,13 @@ __device__ __forceinline__ bool exact_walk(const int32_t *tab, int32_t *s, uint3
     const uint32_t Q = (1u << log_len) >> LOGU;
     uint64_t col[S::NR > 1 ? S::NR - 1 : 1];
     int64_t colt;
-    // the abort word is read every 2^16 states (every chunk for longer ones)
+    // the host-mapped abort word is read once per 2^16 states (per chunk for
+    // longer chunks), from the thread's second period on: threads of a short
+    // launch never read it, so thousands of warps do not queue on one
+    // host-memory word before their work starts
     const uint64_t poll = log_len >= 16 ? 0 : (1ull << (16 - log_len)) - 1;
     for (uint64_t c = c_begin; c < c_end; c++) {
-        if (((c - c_begin) & poll) == 0 && *abort_flag) return false;
+        if (c != c_begin && ((c - c_begin) & poll) == 0 && *abort_flag) return false;
         const uint32_t hib = (uint32_t)(c & 1) << log_len;
         for (uint32_t q = 0; q < Q; q++) {
             const uint32_t g32 = (q << LOGU) | hib;
@@ -271,13 +274,31 @@ __device__ __forceinline__ void exact_epilogue(long long (*red)[NL], bool any_ab
     if (threadIdx.x == 0 && any_abort) atomicExch(status, 1);
 }
 
+// Programmatic dependent launch of the finishing kernel: with
+// EXACT_FINISH_PDL the walk kernels signal at their start that the
+// dependent grid may be scheduled, the finishing kernel is launched with
+// programmatic stream serialisation and its block waits (griddepcontrol.wait)
+// until the walk grid has completed and its writes are visible.  The
+// dependent grid is scheduled only after every walk block has started, so
+// it never takes a slot a walk block is waiting for; its launch latency
+// overlaps the walk instead of following it.
+#ifndef EXACT_FINISH_PDL
+#define EXACT_FINISH_PDL 1
+#endif
+__device__ __forceinline__ void exact_allow_dependents() {
+#if EXACT_FINISH_PDL
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+#endif
+}
+
 // Launches the finishing kernel on `stream` after an exact or 0/1 kernel of
 // `blocks` blocks: out[0..nl) = the sum of the slots (or acc, re-zeroed,
-// when part is nullptr), out[nl] = *status, then *status = 0, so the next
+// when part is nullptr), out[nl] = *status, then *status = 0 and, when
+// given, *counter = 0 (the 0/1 kernel's chunk-group counter), so the next
 // launch starts clean without a memset (pg_exact.cu).
 cudaError_t exact_finish(const unsigned long long *part, int blocks, int nl,
                          unsigned long long *acc, int *status, unsigned long long *out,
-                         cudaStream_t stream);
+                         cudaStream_t stream, unsigned long long *counter = nullptr);
 
 template <int N, int G, int FR = 0>
 __global__ void __launch_bounds__(256, exact_min_blocks(N))
@@ -286,6 +307,7 @@ exact_glynn_kernel(ExactArgs a) {
     constexpr int NP = S::NP, NL = S::NL, NCOL = N - 1;
     extern __shared__ int4 esmem[];
     int32_t *tab = reinterpret_cast<int32_t *>(esmem);
+    exact_allow_dependents();
     for (int i = threadIdx.x; i < NCOL * 2 * NP / 4; i += blockDim.x)
         esmem[i] = reinterpret_cast<const int4 *>(a.tab)[i];
     __syncthreads();

@@ -137,10 +137,13 @@ glynn_m32_kernel(M32Args a) {
         }
     }
 
-    // the abort word is read every 2^16 states (every chunk for longer ones)
+    // the host-mapped abort word is read once per 2^16 states (per chunk for
+    // longer chunks), from the thread's second period on: threads of a short
+    // launch never read it, so thousands of warps do not queue on one
+    // host-memory word before their work starts
     const uint64_t poll = a.log_len >= 16 ? 0 : (1ull << (16 - a.log_len)) - 1;
     for (uint64_t c = c_begin; c < c_end; c++) {
-        if (((c - c_begin) & poll) == 0 && *a.abort_flag) { aborted = true; break; }
+        if (c != c_begin && ((c - c_begin) & poll) == 0 && *a.abort_flag) { aborted = true; break; }
         // bits 0..log_len of the global state index g = c * 2^log_len + i
         const uint32_t hib = (uint32_t)(c & 1) << a.log_len;
         unsigned long long acc_e = 0, acc_o = 0;

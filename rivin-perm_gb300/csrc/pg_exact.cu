@@ -304,7 +304,12 @@ static bool plan_build_binary(const int64_t *A, int n, ExactPlan *P) {
 __global__ void __launch_bounds__(256) exact_finish_kernel(const unsigned long long *part,
                                                            int blocks, int nl,
                                                            unsigned long long *acc, int *status,
-                                                           unsigned long long *out) {
+                                                           unsigned long long *out,
+                                                           unsigned long long *counter) {
+#if EXACT_FINISH_PDL
+    // launched as a programmatic dependent: wait for the walk grid's writes
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+#endif
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int l = warp; l < nl; l += nw) {
         long long t = 0;
@@ -321,14 +326,30 @@ __global__ void __launch_bounds__(256) exact_finish_kernel(const unsigned long l
     if (threadIdx.x == 0) {
         out[nl] = (unsigned long long)(unsigned)*status;
         *status = 0;
+        if (counter) *counter = 0;
     }
 }
 
 cudaError_t exact_finish(const unsigned long long *part, int blocks, int nl,
                          unsigned long long *acc, int *status, unsigned long long *out,
-                         cudaStream_t stream) {
-    exact_finish_kernel<<<1, 256, 0, stream>>>(part, blocks, nl, acc, status, out);
+                         cudaStream_t stream, unsigned long long *counter) {
+#if EXACT_FINISH_PDL
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(1);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, exact_finish_kernel, part, blocks, nl, acc, status, out,
+                              counter);
+#else
+    exact_finish_kernel<<<1, 256, 0, stream>>>(part, blocks, nl, acc, status, out, counter);
     return cudaGetLastError();
+#endif
 }
 
 // Per-block word slots after the result words (the kernels' epilogue);
@@ -446,6 +467,8 @@ static int plan_launch(ExactPlan *P, cudaStream_t stream) {
         b.acc = (unsigned long long *)(P->dev + P->off_acc);
         b.status = (int *)(P->dev + P->off_status);
         b.part = (unsigned long long *)(P->dev + P->off_part);
+        // the chunk-group counter shares the status slot's second 8 bytes
+        b.next = (unsigned long long *)(P->dev + P->off_status + 8);
         b.abort_flag = P->abort_dev;
         b.chunks = P->chunks.chunks;
         b.log_len = P->chunks.log_len;
@@ -457,7 +480,7 @@ static int plan_launch(ExactPlan *P, cudaStream_t stream) {
         PG_CUDA(launch_binary_any(P->npad, P->G, P->planes, P->words_tracked, b, split,
                                   (int)P->blocks, stream));
         PG_CUDA(exact_finish(b.part, (int)P->blocks, P->NL, b.acc, b.status,
-                             (unsigned long long *)(P->dev + P->off_out), stream));
+                             (unsigned long long *)(P->dev + P->off_out), stream, b.next));
         return PG_OK;
     }
     ExactArgs args;

@@ -83,10 +83,11 @@ __global__ void __launch_bounds__(256) mod3_kernel(Mod3Args a) {
         for (int j = 0; j < n; j++)
             if ((gs >> j) & 1) f3_add(m, s, cm_s[j], cs_s[j]);
         const uint32_t blocks = (1u << a.log_len) >> LOGU;
-        // the abort word is read every 2^20 subsets (every chunk for longer ones)
+        // the host-mapped abort word is read once per 2^20 subsets (per chunk
+        // for longer chunks), from the thread's second period on
         const uint64_t poll = a.log_len >= 20 ? 0 : (1ull << (20 - a.log_len)) - 1;
         for (uint64_t c = c_begin; c < c_end; c++) {
-            if (((c - c_begin) & poll) == 0 && *a.abort_flag) {
+            if (c != c_begin && ((c - c_begin) & poll) == 0 && *a.abort_flag) {
                 aborted = true;
                 break;
             }

@@ -70,10 +70,11 @@ __global__ void __launch_bounds__(POLY_WIDE_BT) affine_wide_kernel(PolyArgs a, i
         }
     }
     const uint32_t len = 1u << a.log_len;
-    // the abort word is read every 2^12 states (every chunk for longer ones)
+    // the host-mapped abort word is read once per 2^12 states (per chunk for
+    // longer chunks), from the thread's second period on
     const uint64_t poll = a.log_len >= 12 ? 0 : (1ull << (12 - a.log_len)) - 1;
     for (uint64_t c = c_begin; c < c_end; c++) {
-        if (((c - c_begin) & poll) == 0 && *a.abort_flag) {
+        if (c != c_begin && ((c - c_begin) & poll) == 0 && *a.abort_flag) {
             aborted = true;
             break;
         }

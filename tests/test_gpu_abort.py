@@ -1,7 +1,8 @@
 """Host-side abort of long launches: pg_abort() called from another host
 thread while a multi-second traversal runs makes the call return PG_EABORT
 within a fraction of a second (the kernels read the host-mapped abort word
-every 2^16 states, or every chunk); pg_clear_abort() re-arms the library and
+once per 2^16 states, or per chunk, after each thread's first period);
+pg_clear_abort() re-arms the library and
 the next call computes the right value.  The failure is made on the host:
 no kernel is broken, nothing waits on anything that is not set."""
 
@@ -53,15 +54,22 @@ def test_abort_residue_engine(lib):
 
 
 def test_abort_flag_left_set_stops_the_next_launch_at_once(lib):
-    # a raised word that nobody cleared makes every later launch stop at its
-    # first poll; clearing it restores normal service
-    a = np.random.default_rng(9).integers(-8, 9, (20, 20), dtype=np.int64)
+    # a raised word that nobody cleared makes every later long launch stop at
+    # its first poll (after each thread's first 2^16 states: a 36 x 36 walk
+    # gives every thread several hundred thousand); clearing it restores
+    # normal service.  Launches too short for a poll complete as usual.
+    a = np.random.default_rng(9).integers(-8, 9, (36, 36), dtype=np.int64)
     h = lib.load()
     h.pg_abort()
     try:
+        t0 = time.perf_counter()
         with pytest.raises(lib.PermGpuError) as err:
             lib.exact_permanent(a, lib.exact_limbs(a))
         assert err.value.status == lib.PG_EABORT
+        assert time.perf_counter() - t0 < 1.0
+        b = np.random.default_rng(10).integers(-8, 9, (16, 16), dtype=np.int64)
+        assert lib.exact_permanent(b, lib.exact_limbs(b)) == oracle.exact_permanent(b.tolist())
     finally:
         h.pg_clear_abort()
-    assert lib.exact_permanent(a, lib.exact_limbs(a)) == oracle.exact_permanent(a.tolist())
+    c = np.random.default_rng(9).integers(-8, 9, (20, 20), dtype=np.int64)
+    assert lib.exact_permanent(c, lib.exact_limbs(c)) == oracle.exact_permanent(c.tolist())
