@@ -45,8 +45,10 @@ const char *pg_last_error(void);
 /* SM count and compute capability of the current device. */
 int pg_device_info(int *sm_count, int *cc_major, int *cc_minor);
 
-/* Ask running launches to stop at their next chunk boundary; they return
- * PG_EABORT.  pg_clear_abort() re-arms the library. */
+/* Ask running launches to stop at their next poll; they return PG_EABORT.
+ * A kernel thread reads the abort word once per 2^16 states (per chunk
+ * for longer chunks) from its second period on, so launches whose threads
+ * walk fewer states complete.  pg_clear_abort() re-arms the library. */
 void pg_abort(void);
 void pg_clear_abort(void);
 

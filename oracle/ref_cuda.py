@@ -363,11 +363,20 @@ def binary_modp(matrix, p: int, stream=None, timer=None) -> int:
             trans[direction, v + B_MAX_ORDER] = ratio * one_mont % p
     d = driver()
     f, fname = d.function_containing("binary", "binary_glynn_ratio_kernel")
-    # constants live in the kernel's anonymous namespace: same tag
-    tag = fname[:fname.index("25binary_glynn_ratio_kernel")]
+    # The constants live in the kernel's anonymous namespace; in device code
+    # their names are also wrapped in the translation unit's internal
+    # namespace: _ZN <_INTERNAL_H> <_GLOBAL__N__H> <name> E, H taken from
+    # the kernel's name _ZN <len> _GLOBAL__N__H ...
+    i = 3
+    while fname[i].isdigit():
+        i += 1
+    ns = fname[i:i + int(fname[3:i])]
+    h = ns[len("_GLOBAL__N__"):]
+    internal = "_INTERNAL_" + h
 
     def cname(name):
-        return [f"{tag}L{len(name)}{name}E", f"{tag}{len(name)}{name}E"]
+        return [f"_ZN{len(internal)}{internal}{len(ns)}{ns}{len(name)}{name}E",
+                f"_ZN{len(ns)}{ns}L{len(name)}{name}E", f"_ZN{len(ns)}{ns}{len(name)}{name}E"]
     off = np.zeros(B_MAX_ORDER, np.uint16)
     off[:len(offsets)] = offsets
     rw = np.zeros(B_MAX_ORDER * B_MAX_ORDER, np.uint8)
@@ -558,7 +567,7 @@ def main(argv=None):
         mats = workloads.float28(256)[: args.f64_sample]
         t = Timer()
         vals = [parallel_real(m, stream, t) for m in mats]
-        ours, _ = _lib.glynn_f64_fwd_bwd(np.asarray(mats), want_grad=False)
+        ours, _, _ = _lib.glynn_f64_fwd_bwd(np.asarray(mats), want_grad=False)
         err = max(abs(v - float(o)) / max(1e-300, abs(float(o))) for v, o in zip(vals, np.ravel(ours)))
         line(workload="float28 forward", reference_kernel="permanent_glynn_kernel<false> (permanent_parallel_real)",
              matrices=len(mats), device_ms_per_matrix=t.ms, est_s_for_256=256 * sum(t.ms) / len(t.ms) / 1e3,

@@ -49,7 +49,8 @@ struct BinaryArgs {
     int *status;
     unsigned long long *part;  // [NL][gridDim] per-block slots (exact_epilogue), or nullptr
     unsigned long long *next;  // chunk groups taken so far beyond each warp's first; zero at
-                               // launch, re-zeroed by the finishing kernel
+                               // launch, re-zeroed by the finishing kernel; nullptr: warp w
+                               // walks groups w, w + warps, w + 2 warps, ...
     volatile const int *abort_flag;
     uint64_t chunks;
     int log_len;
@@ -158,14 +159,16 @@ binary_glynn_kernel(BinaryArgs a) {
     // Chunks are dealt in groups of 32 consecutive ones, lane l of a warp
     // taking the group's chunk l (so the step's column is warp-uniform and
     // every lane runs the same loop count, which the ballots need).  Each
-    // warp walks its own group first and then takes the next untaken group
-    // from a counter, one atomic per 2^(log_len + 5) states.  The share of
-    // surviving states, and so the exact evaluations, varies strongly along
-    // the walk with the signs of the columns: a fixed deal (contiguous
-    // ranges, or round-robin with a stride that is a multiple of 2^12
-    // chunks, which pins twelve column signs per warp) left some SMs with
-    // 40 % more instructions than the mean.  Each chunk starts from a
-    // closed-form tracker state.
+    // warp walks its own group first and then, when survivors are common,
+    // takes the next untaken group from a counter, one atomic per
+    // 2^(log_len + 5) states.  The share of surviving states, and so the
+    // exact evaluations, varies strongly along the walk with the signs of
+    // the columns: a fixed deal (contiguous ranges, or round-robin with a
+    // stride that is a multiple of 2^12 chunks, which pins twelve column
+    // signs per warp) left some SMs with 40 % more instructions than the
+    // mean.  When survivors are rare the walk dominates, the fixed
+    // round-robin deal is balanced, and it saves the atomics (grid: 446 vs
+    // 454 ms).  Each chunk starts from a closed-form tracker state.
     const uint64_t T = (uint64_t)gridDim.x * blockDim.x;
     const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const uint64_t ngroups = (a.chunks + 31) >> 5;
@@ -232,6 +235,10 @@ binary_glynn_kernel(BinaryArgs a) {
             aborted = true;
             break;
         }
+        // the next group is taken now and used after this one, so the
+        // atomic's round trip overlaps the walk
+        unsigned long long nx = 0;
+        if (a.next && lane == 0) nx = (T >> 5) + atomicAdd(a.next, 1ull);
         const uint64_t ci = (grp << 5) + lane;
         const bool act = ci < a.chunks;
         const uint64_t c = a.chunk0 + ci;
@@ -275,9 +282,7 @@ binary_glynn_kernel(BinaryArgs a) {
             evaluate(true);
             qn = 0;
         }
-        unsigned long long nx = 0;
-        if (lane == 0) nx = (T >> 5) + atomicAdd(a.next, 1ull);
-        grp = __shfl_sync(0xffffffffu, nx, 0);
+        grp = a.next ? __shfl_sync(0xffffffffu, nx, 0) : grp + (T >> 5);
     }
     if (qn > 0) evaluate(true);
     if (terms > 0) FoldCols<NR, NL>::apply(acc, col, colt);

@@ -467,8 +467,9 @@ static int plan_launch(ExactPlan *P, cudaStream_t stream) {
         b.acc = (unsigned long long *)(P->dev + P->off_acc);
         b.status = (int *)(P->dev + P->off_status);
         b.part = (unsigned long long *)(P->dev + P->off_part);
-        // the chunk-group counter shares the status slot's second 8 bytes
-        b.next = (unsigned long long *)(P->dev + P->off_status + 8);
+        // the chunk-group counter (taken only when survivors are common)
+        // shares the status slot's second 8 bytes
+        b.next = P->bin_split ? (unsigned long long *)(P->dev + P->off_status + 8) : nullptr;
         b.abort_flag = P->abort_dev;
         b.chunks = P->chunks.chunks;
         b.log_len = P->chunks.log_len;
