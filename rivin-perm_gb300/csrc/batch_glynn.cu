@@ -120,7 +120,13 @@ __global__ void __launch_bounds__(256, 2) batch_glynn_kernel(BatchArgs a) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     int32_t *wtab = reinterpret_cast<int32_t *>(bsmem) + warp * BATCH_SLICE;
     uint32_t cur = 0xffffffffu;
-    for (;;) {
+    for (unsigned int k = 0;; k++) {
+        // the host-mapped abort word, once per 8 tasks of the warp (a task's
+        // own walk reads it only past 2^16 states per lane)
+        if (k != 0 && (k & 7) == 0 && __any_sync(0xffffffffu, *a.abort_flag != 0)) {
+            if (lane == 0) atomicExch(a.status, 1);
+            break;
+        }
         unsigned int ti = 0;
         if (lane == 0) ti = atomicAdd(a.counter, 1u);
         ti = __shfl_sync(0xffffffffu, ti, 0);

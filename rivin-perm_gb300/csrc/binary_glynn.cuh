@@ -48,8 +48,9 @@ struct BinaryArgs {
     unsigned long long *acc;   // [NL] per-word sums (exact kernel layout)
     int *status;
     unsigned long long *part;  // [NL][gridDim] per-block slots (exact_epilogue), or nullptr
-    unsigned long long *next;  // chunk groups taken so far beyond each warp's first; zero at
-                               // launch, re-zeroed by the finishing kernel; nullptr: warp w
+    unsigned long long *next;  // chunk groups taken so far beyond each warp's first (the
+                               // split instantiation): zero at launch, re-zeroed by the
+                               // finishing kernel; unused without the split, where warp w
                                // walks groups w, w + warps, w + 2 warps, ...
     volatile const int *abort_flag;
     uint64_t chunks;
@@ -159,9 +160,9 @@ binary_glynn_kernel(BinaryArgs a) {
     // Chunks are dealt in groups of 32 consecutive ones, lane l of a warp
     // taking the group's chunk l (so the step's column is warp-uniform and
     // every lane runs the same loop count, which the ballots need).  Each
-    // warp walks its own group first and then, when survivors are common,
-    // takes the next untaken group from a counter, one atomic per
-    // 2^(log_len + 5) states.  The share of surviving states, and so the
+    // warp walks its own group first and then, in the split instantiation
+    // (survivors common), takes the next untaken group from a counter, one
+    // atomic per 2^(log_len + 5) states.  The share of surviving states, and so the
     // exact evaluations, varies strongly along the walk with the signs of
     // the columns: a fixed deal (contiguous ranges, or round-robin with a
     // stride that is a multiple of 2^12 chunks, which pins twelve column
@@ -229,8 +230,11 @@ binary_glynn_kernel(BinaryArgs a) {
         __syncwarp();
     };
 
-    uint64_t grp = tid >> 5;              // the warp's own group first
-    for (uint64_t k = 0; grp < ngroups; k++) {
+    // split: group grp (the warp's own first, then from the counter);
+    // otherwise round k of the round-robin deal (chunk k T + tid)
+    const uint64_t kmax = (a.chunks + T - 1) / T;
+    uint64_t grp = tid >> 5;
+    for (uint64_t k = 0; SPLIT ? grp < ngroups : k < kmax; k++) {
         if (k != 0 && (k & poll) == 0 && __any_sync(0xffffffffu, *a.abort_flag != 0)) {
             aborted = true;
             break;
@@ -238,8 +242,10 @@ binary_glynn_kernel(BinaryArgs a) {
         // the next group is taken now and used after this one, so the
         // atomic's round trip overlaps the walk
         unsigned long long nx = 0;
-        if (a.next && lane == 0) nx = (T >> 5) + atomicAdd(a.next, 1ull);
-        const uint64_t ci = (grp << 5) + lane;
+        if constexpr (SPLIT) {
+            if (lane == 0) nx = (T >> 5) + atomicAdd(a.next, 1ull);
+        }
+        const uint64_t ci = SPLIT ? (grp << 5) + lane : k * T + tid;
         const bool act = ci < a.chunks;
         const uint64_t c = a.chunk0 + ci;
         if (act) init_tracker(c << a.log_len);
@@ -282,7 +288,7 @@ binary_glynn_kernel(BinaryArgs a) {
             evaluate(true);
             qn = 0;
         }
-        grp = a.next ? __shfl_sync(0xffffffffu, nx, 0) : grp + (T >> 5);
+        if constexpr (SPLIT) grp = __shfl_sync(0xffffffffu, nx, 0);
     }
     if (qn > 0) evaluate(true);
     if (terms > 0) FoldCols<NR, NL>::apply(acc, col, colt);

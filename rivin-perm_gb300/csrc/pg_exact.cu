@@ -467,9 +467,9 @@ static int plan_launch(ExactPlan *P, cudaStream_t stream) {
         b.acc = (unsigned long long *)(P->dev + P->off_acc);
         b.status = (int *)(P->dev + P->off_status);
         b.part = (unsigned long long *)(P->dev + P->off_part);
-        // the chunk-group counter (taken only when survivors are common)
-        // shares the status slot's second 8 bytes
-        b.next = P->bin_split ? (unsigned long long *)(P->dev + P->off_status + 8) : nullptr;
+        // the chunk-group counter of the split instantiation shares the
+        // status slot's second 8 bytes
+        b.next = (unsigned long long *)(P->dev + P->off_status + 8);
         b.abort_flag = P->abort_dev;
         b.chunks = P->chunks.chunks;
         b.log_len = P->chunks.log_len;
@@ -481,7 +481,8 @@ static int plan_launch(ExactPlan *P, cudaStream_t stream) {
         PG_CUDA(launch_binary_any(P->npad, P->G, P->planes, P->words_tracked, b, split,
                                   (int)P->blocks, stream));
         PG_CUDA(exact_finish(b.part, (int)P->blocks, P->NL, b.acc, b.status,
-                             (unsigned long long *)(P->dev + P->off_out), stream, b.next));
+                             (unsigned long long *)(P->dev + P->off_out), stream,
+                             split ? b.next : nullptr));
         return PG_OK;
     }
     ExactArgs args;

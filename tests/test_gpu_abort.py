@@ -53,6 +53,20 @@ def test_abort_residue_engine(lib):
     assert lib.residues(b, [p]) == [oracle.exact_permanent(b.tolist()) % p]
 
 
+def test_abort_batched_engine(lib):
+    # 256 matrices of order 32, entries in [-3, 3]: about 2 s of one
+    # persistent launch; its warps read the word once per 8 tasks
+    mats = [np.random.default_rng(600 + i).integers(-3, 4, (32, 32), dtype=np.int64)
+            for i in range(256)]
+    lib.load().pg_clear_abort()
+    status, took = _aborted_after(lib, lambda: lib.batch_exact(mats))
+    assert status == lib.PG_EABORT
+    assert took < 1.5
+    small = [np.random.default_rng(700 + i).integers(-3, 4, (n, n), dtype=np.int64)
+             for i, n in enumerate((12, 17, 21))]
+    assert lib.batch_exact(small) == [oracle.exact_permanent(m.tolist()) for m in small]
+
+
 def test_abort_flag_left_set_stops_the_next_launch_at_once(lib):
     # a raised word that nobody cleared makes every later long launch stop at
     # its first poll (after each thread's first 2^16 states: a 36 x 36 walk
