@@ -193,6 +193,75 @@ def cpu_sample(matrix, seconds_target: float = 12.0):
     return states / dt, threads, kind, desc
 
 
+def cpu_batch_sample(mats, seconds_target: float = 15.0):
+    """The reference's per-matrix CPU path (oracle port of perm.py:1076-1212:
+    bound, primes from 2^30, Glynn residues on all host cores, CRT) over the
+    batch's matrices in order until about `seconds_target` have passed.
+    Returns (Glynn states/s over the sample, cores, sample description)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    oracle.build()
+    threads = os.cpu_count() or 1
+    done, states = 0, 0
+    t = time.perf_counter()
+    for m in mats:
+        oracle.exact_permanent(m.tolist(), threads)
+        done += 1
+        states += 1 << (m.shape[0] - 1)
+        if time.perf_counter() - t >= seconds_target:
+            break
+    dt = time.perf_counter() - t
+    return states / dt, threads, (f"the first {done} of the {len(mats)} matrices, exact by CRT "
+                                  f"over oracle Glynn residues (all primes from 2^30 up), "
+                                  f"{threads} OpenMP threads")
+
+
+def cpu_f64_sample(mats, seconds_target: float = 15.0):
+    """FP64 Glynn with Kahan summation on the host cores (oracle port of
+    perm_parallel_cuda.cu:68-209, forward only: the reference has no
+    gradient) over the batch's matrices in order until about
+    `seconds_target` have passed."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    oracle.build()
+    threads = os.cpu_count() or 1
+    done, states = 0, 0
+    t = time.perf_counter()
+    for m in mats:
+        oracle.glynn_f64(m, threads)
+        done += 1
+        states += 1 << (m.shape[0] - 1)
+        if time.perf_counter() - t >= seconds_target:
+            break
+    dt = time.perf_counter() - t
+    return states / dt, threads, (f"forward of the first {done} of the {len(mats)} matrices, "
+                                  f"{threads} OpenMP threads")
+
+
+def cpu_binary_sample(matrix, order: int = 32):
+    """The reference's 0/1 ratio-table Glynn (oracle port of
+    perm_binary_omp.c:236-347) for one prime on the host cores, on the
+    leading order x order block of a 40x40 workload matrix (a full 40x40
+    residue is 2^39 states, hours on the host)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import numpy as np
+    import oracle
+    oracle.build()
+    threads = os.cpu_count() or 1
+    sub = np.ascontiguousarray(np.asarray(matrix)[:order, :order], dtype=np.uint8)
+    for i in range(order):                         # no empty row or column
+        if not sub[i].any():
+            sub[i, i] = 1
+        if not sub[:, i].any():
+            sub[i, i] = 1
+    t = time.perf_counter()
+    oracle.binary_mod_p(sub, 2_147_483_647, threads)
+    dt = time.perf_counter() - t
+    return (1 << (order - 1)) / dt, threads, (f"one residue (p = 2^31 - 1) of the leading "
+                                              f"{order}x{order} block of matrix 0, {threads} "
+                                              f"OpenMP threads")
+
+
 def run_reference(args, world, rank):
     import numpy as np
     from permgpu import workloads
@@ -203,8 +272,9 @@ def run_reference(args, world, rank):
         # host cores) in the cpu_baseline field of their gb300 line
         print(json.dumps({"impl": "reference", "unavailable":
                           f"the reference arm times the generic workloads "
-                          f"({', '.join(sorted(WORKLOADS))}); {args.workload} reports its CPU "
-                          f"baseline in the cpu_baseline field of the gb300 line"}))
+                          f"({', '.join(sorted(WORKLOADS))}); batch4096, float28, binary40, "
+                          f"rook28 and mod3_40 report their CPU baseline in the cpu_baseline "
+                          f"field of the gb300 line"}))
         return
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle
@@ -539,6 +609,7 @@ def run_gpu_batch(args, world, rank, local):
     value = world * states / (step_ms * 1e-3)
     e2e_s = max_over_ranks(world, statistics.mean(e2e))
     packed, _, _ = _lib.pack_batch(mats)
+    cpu = cpu_batch_sample(mats, args.cpu_seconds) if rank == 0 and not args.no_cpu else None
     if rank == 0:
         print(json.dumps({
             "metric": "batched Glynn steps/s (4096 uneven int matrices, exact)", "value": value,
@@ -549,6 +620,9 @@ def run_gpu_batch(args, world, rank, local):
                                    "numpy default_rng(4)", "states": states, "tune": list(tune),
                        "tasks": plan.tasks, "blocks": plan.blocks, "graph_captured": True,
                        "l2": "flushed between timed steps (256 MiB write)"},
+            "cpu_baseline": None if cpu is None else {
+                "value": cpu[0], "unit": "steps/s", "cores": cpu[1], "kind": "port",
+                "sample": cpu[2], "est_s_for_batch": states / cpu[0], "host": host_info()},
             "speedup_vs_plain_exact_loop": t_loop_exact / (step_ms * 1e-3),
             "speedup_vs_plain_residue_loop": t_loop_res / (step_ms * 1e-3),
             "plain_exact_loop_s": t_loop_exact, "plain_residue_loop_s": t_loop_res,
@@ -672,6 +746,7 @@ def run_gpu_float28(args, world, rank, local):
     step_ms = max_over_ranks(world, statistics.mean(ms))
     e2e_s = max_over_ranks(world, statistics.mean(e2e))
     fwd_ms = statistics.mean(ms_fwd)
+    cpu = cpu_f64_sample(A_host, args.cpu_seconds) if rank == 0 and not args.no_cpu else None
     # roofline: FP32-pipe instructions of the algorithm per state, counted
     # from the kernel source for the n live rows (lanes): one double-float
     # add per row update (11 FP32 instructions), 10 double-float products in
@@ -704,6 +779,9 @@ def run_gpu_float28(args, world, rank, local):
             "tolerance": 1e-10,
             "forward_only_ms": fwd_ms,
             "gradient_cost_ratio": step_ms / fwd_ms,
+            "cpu_baseline": None if cpu is None else {
+                "value": cpu[0], "unit": "steps/s (forward)", "cores": cpu[1], "kind": "port",
+                "sample": cpu[2], "est_s_forward_for_batch": states / cpu[0], "host": host_info()},
             "roofline": {"bound": "fp32 issue", "achieved": achieved / 1e12, "peak": fma32 / 1e12,
                          "unit": "Tops/s", "frac": achieved / fma32, "traffic": None,
                          "peak_source": "measured live: pg_probe_int_throughput fma.rn.f32",
@@ -974,6 +1052,17 @@ def run_gpu_exact_set(args, world, rank, local):
     barrier(world)
     clk = clocks.stop()
     step_s = max_over_ranks(world, statistics.mean(ts))
+    cpu = None
+    if rank == 0 and args.workload == "binary40" and not args.no_cpu:
+        rate, cores, sample = cpu_binary_sample(mats[0])
+        from permgpu import binary
+        from permgpu.crt import binary_primes_above
+        k = [len(binary_primes_above(binary.binary_permanent_bound(m.tolist()))) for m in mats]
+        cpu = {"value": rate, "unit": "steps/s (one prime)", "cores": cores, "kind": "port",
+               "sample": sample,
+               "est_s_for_set": sum(kk * (1 << 39) for kk in k) / rate,
+               "estimate": f"{sum(k)} residues of 2^39 states at the sampled rate",
+               "host": host_info()}
     if rank == 0 and args.workload == "schur41":
         n = args.order
         # published: perm(S_41) by the reference's CUDA necklace kernel in
@@ -1020,6 +1109,7 @@ def run_gpu_exact_set(args, world, rank, local):
             "time_to_exact_s": step_s, "results": [str(v) for v in got],
             "result_checked_against_reference": check_method is not None,
             "result_check": check_method,
+            "cpu_baseline": cpu,
             "e2e": {"value": world * states / step_s, "unit": "steps/s",
                     "h2d_bytes_per_step": None, "d2h_bytes_per_step": None,
                     "note": "whole-call API timed end to end (host inputs, host results)"},
