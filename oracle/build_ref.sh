@@ -26,18 +26,25 @@ export TMPDIR="$HERE/.tmp"      # the compiler's temporary files stay in the tre
 PYINC="$(python3 -c 'import sysconfig; print(sysconfig.get_paths()["include"])')"
 NPINC="$(python3 -c 'import numpy; print(numpy.get_include())')"
 SUFFIX="$(python3 -c 'import sysconfig; print(sysconfig.get_config_var("EXT_SUFFIX"))')"
-gcc -O3 -fopenmp -fPIC -shared -I"$PYINC" "$REF/perm_c_omp.c" -o "$OUT/perm_c_ext$SUFFIX" &
-gcc -O3 -fopenmp -fPIC -shared -I"$PYINC" "$REF/perm_binary_omp.c" -o "$OUT/perm_binary_ext$SUFFIX" &
-gcc -O3 -std=c11 -fopenmp -fPIC -shared -I"$PYINC" "$REF/perm_polynomial_omp.c" \
-    -o "$OUT/perm_polynomial_ext$SUFFIX" &
-gcc -O3 -fopenmp -fPIC -shared -I"$PYINC" -I"$NPINC" "$REF/perm_mod3_omp.c" \
-    -o "$OUT/perm_mod3_omp$SUFFIX" &
+# outputs newer than their source are kept
+fresh() { [ -f "$2" ] && [ "$2" -nt "$1" ]; }
+fresh "$REF/perm_c_omp.c" "$OUT/perm_c_ext$SUFFIX" ||
+  gcc -O3 -fopenmp -fPIC -shared -I"$PYINC" "$REF/perm_c_omp.c" -o "$OUT/perm_c_ext$SUFFIX" &
+fresh "$REF/perm_binary_omp.c" "$OUT/perm_binary_ext$SUFFIX" ||
+  gcc -O3 -fopenmp -fPIC -shared -I"$PYINC" "$REF/perm_binary_omp.c" -o "$OUT/perm_binary_ext$SUFFIX" &
+fresh "$REF/perm_polynomial_omp.c" "$OUT/perm_polynomial_ext$SUFFIX" ||
+  gcc -O3 -std=c11 -fopenmp -fPIC -shared -I"$PYINC" "$REF/perm_polynomial_omp.c" \
+      -o "$OUT/perm_polynomial_ext$SUFFIX" &
+fresh "$REF/perm_mod3_omp.c" "$OUT/perm_mod3_omp$SUFFIX" ||
+  gcc -O3 -fopenmp -fPIC -shared -I"$PYINC" -I"$NPINC" "$REF/perm_mod3_omp.c" \
+      -o "$OUT/perm_mod3_omp$SUFFIX" &
 # the reference's CUDA kernels, device code only (cubins for sm_103a, loaded
 # through the CUDA driver API by oracle/ref_cuda.py; the host code around
 # them is restated there)
 if command -v nvcc > /dev/null; then
   for f in perm_modp_cuda perm_binary_cuda perm_parallel_cuda; do
-    nvcc -gencode arch=compute_103a,code=sm_103a -O3 -cubin "$REF/$f.cu" -o "$OUT/$f.cubin" &
+    fresh "$REF/$f.cu" "$OUT/$f.cubin" ||
+      nvcc -gencode arch=compute_103a,code=sm_103a -O3 -cubin "$REF/$f.cu" -o "$OUT/$f.cubin" &
   done
 fi
 wait
