@@ -749,12 +749,13 @@ def run_gpu_float28(args, world, rank, local):
     cpu = cpu_f64_sample(A_host, args.cpu_seconds) if rank == 0 and not args.no_cpu else None
     # roofline: FP32-pipe instructions of the algorithm per state, counted
     # from the kernel source for the n live rows (lanes): one double-float
-    # add per row update (11 FP32 instructions), 10 double-float products in
-    # the 5-level butterfly (7 each), one add for the forward term and 1 + M
-    # (M = 4) for the gradient columns; the forward-only walk drops the
-    # gradient's 5 products (E) and 5 adds
-    df_add, df_mul = 11, 7
-    fwd_bwd_ops = n * (df_add * (1 + 1 + 1 + 4) + df_mul * 10)
+    # add per row update (11 FP32 instructions), 5 double-float products in
+    # the butterfly for the full product (7 each), one double-float division
+    # for the all-but-self product (10 FP32 instructions and a reciprocal),
+    # one add for the forward term and 1 + M (M = 4) for the gradient
+    # columns; the forward-only walk drops the division and 5 adds
+    df_add, df_mul, df_div = 11, 7, 10
+    fwd_bwd_ops = n * (df_add * (1 + 1 + 1 + 4) + df_mul * 5 + df_div)
     fwd_ops = n * (df_add * 2 + df_mul * 5)
     achieved = states * fwd_bwd_ops / (step_ms * 1e-3)
     achieved_fwd = states * fwd_ops / (fwd_ms * 1e-3)

@@ -361,8 +361,7 @@ int pg_glynn_window(const double *Are, const double *Aim, int n, uint64_t lo,
  * All calls share the scratch: calls that overlap on the GPU race and must
  * be serialised by the caller.  The first call on each device looks up the
  * scratch address (cudaGetSymbolAddress) and keeps it for the process's
- * life; that first call should come before any stream capture, and calls
- * after cudaDeviceReset are not supported.  pg_abort() stops it only once
+ * life; calls after cudaDeviceReset are not supported.  pg_abort() stops it only once
  * the process's abort word exists (any allocating entry point, pg_abort or
  * pg_clear_abort creates it; this entry point does not).
  */

@@ -40,6 +40,25 @@ __device__ __forceinline__ df df_mul(df a, df b) {
     r.lo = e - (r.hi - p);
     return r;
 }
+// a / b by long division in two FP32 digits (Dekker 1971; the double-float
+// quotient of Hida, Li and Bailey's QD library): q1 = a.hi / b.hi from the
+// FP32 reciprocal, the remainder a - q1 b with the exact error of q1 b.hi
+// from an FMA, then the correction digit q2 = remainder / b.hi.  Relative
+// error about 2^-45 for normal operands; b must be well away from zero (the
+// callers check it).
+__device__ __forceinline__ df df_div(df a, df b) {
+    const float r = __frcp_rn(b.hi);
+    const float q1 = a.hi * r;
+    const float p = q1 * b.hi;
+    const float pe = fmaf(q1, b.hi, -p);
+    float rem = (a.hi - p) - pe;
+    rem = fmaf(-q1, b.lo, rem + a.lo);
+    const float q2 = rem * r;
+    df res;
+    res.hi = q1 + q2;
+    res.lo = q2 - (res.hi - q1);
+    return res;
+}
 __device__ __forceinline__ df df_shfl_xor(df a, int off) {
     return df{__shfl_xor_sync(0xffffffffu, a.hi, off), __shfl_xor_sync(0xffffffffu, a.lo, off)};
 }

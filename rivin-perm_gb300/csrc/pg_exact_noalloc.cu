@@ -26,9 +26,9 @@
 //     serialise them;
 //   * the first call on a device looks up the array's device address with
 //     cudaGetSymbolAddress (once per device, that device current) and keeps
-//     it for the life of the process; make that first call before any
-//     stream capture begins.  Calls after cudaDeviceReset on that device
-//     are not supported (the cached address belongs to the old context);
+//     it for the life of the process.  Calls after cudaDeviceReset on that
+//     device are not supported (the cached address belongs to the old
+//     context);
 //   * the call copies the inputs from and the result to host memory and
 //     synchronises `stream` before it returns;
 //   * pg_abort() reaches this entry point only when the process-wide abort

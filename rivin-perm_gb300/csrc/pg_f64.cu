@@ -118,14 +118,27 @@ __global__ void __launch_bounds__(128) glynn_f64_kernel(F64Args a) {
                     const df d = tab[wib][j][lane];
                     if (live) s = df_add(s, sub ? df_neg(d) : d);
                 }
-                // butterfly: T = prod_l s_l, E = prod_{l != lane} s_l (the
-                // all-but-self products only when the gradient is wanted)
+                // butterfly: T = prod_l s_l.  The all-but-self products
+                // E = prod_{l != lane} s_l (gradient only) are T / s_l, one
+                // double-float division instead of five more products, unless
+                // some row sum is zero or tiny (|s| < 2^-24: then T could
+                // have lost what E keeps), where a second product butterfly
+                // gives them directly.
                 df T = s, E = df{1.f, 0.f};
 #pragma unroll
-                for (int lv = 0; lv < LEV; lv++) {
-                    const df o = df_shfl_xor(T, 1 << lv);
-                    if (GRAD) E = df_mul(E, o);
-                    T = df_mul(T, o);
+                for (int lv = 0; lv < LEV; lv++) T = df_mul(T, df_shfl_xor(T, 1 << lv));
+                if (GRAD) {
+                    if (!__any_sync(0xffffffffu, fabsf(s.hi) < 5.9604645e-8f)) {
+                        E = df_div(T, s);
+                    } else {
+                        df U = s;
+#pragma unroll
+                        for (int lv = 0; lv < LEV; lv++) {
+                            const df o = df_shfl_xor(U, 1 << lv);
+                            E = df_mul(E, o);
+                            U = df_mul(U, o);
+                        }
+                    }
                 }
                 const bool odd = g & 1;                // Glynn sign (-1)^g
                 const df term = odd ? df_neg(T) : T;
