@@ -267,6 +267,120 @@ def glynn_modp(matrix, p: int, stream=None, timer=None) -> int:
     return r * pow((p >> 1) + 1, n - 1, p) % p        # 2^(1-n), perm_modp_cuda.cu:1242-1246
 
 
+# --- perm_modp_cuda.cu: Schur necklace kernel -----------------------------
+
+NECKLACE_CONFIG = {40: (24, 256, 4), 46: (28, 256, 4)}   # perm_modp_cuda.cu:923-930
+NECKLACE_TASK = np.dtype([("word", "<u8"), ("period", "<u4"), ("weight", "<u4")])
+
+
+def k_necklace(m: int, depth: int) -> str:                    # perm_modp_cuda.cu:618
+    return (f"_Z26schur_necklace_pm32_kernelILi{m}ELi{depth}EEvPK18NecklacePrefixTask"
+            f"jPKjjjjPjPy")
+
+
+def necklace_frontier(m: int, depth: int) -> np.ndarray:
+    """perm_modp_cuda.cu:91-147 (build_necklace_frontier): FKM prefixes of
+    length `depth` of pre-necklaces of length m with weight <= m/2, each with
+    its period and weight, the word left-aligned to m bits."""
+    tasks = []
+    bits = [0] * 64
+
+    def rec(position, period, weight, prefix):
+        if position > depth:
+            tasks.append((prefix << (m - depth), period, weight))
+            return
+        copied = bits[position - period]
+        if weight + copied <= m // 2:
+            bits[position] = copied
+            rec(position + 1, period, weight + copied, (prefix << 1) | copied)
+        if copied == 0 and weight + 1 <= m // 2:
+            bits[position] = 1
+            rec(position + 1, position, weight + 1, (prefix << 1) | 1)
+    rec(1, 1, 0, 0)
+    return np.array(tasks, dtype=NECKLACE_TASK)
+
+
+_frontiers = {}
+
+
+def _smallest_primitive_root_prime(n: int) -> int:         # perm_modp_cuda.cu:151-165
+    for g in range(2, n):
+        v, ok = 1, True
+        for _ in range(1, n - 1):
+            v = v * g % n
+            if v == 1:
+                ok = False
+                break
+        if ok:
+            return g
+    raise ValueError("no primitive root")
+
+
+def schur_necklace_modp(n: int, omega: int, p: int, stream=None, timer=None) -> int:
+    """perm_modp_cuda.cu:970-1111 (schur_necklace_modp_cuda_internal):
+    perm(S_n) mod p for prime n with n - 1 in {40, 46}, p = 2^32 - c
+    (1 <= c < 2^16) and omega^n == 1, by the reference's persistent necklace
+    kernel over its FKM frontier."""
+    import torch
+    m = n - 1
+    gap = (1 << 32) - p
+    if (n < 3 or n % 2 == 0 or m not in NECKLACE_CONFIG or p % 2 == 0 or p > 0xFFFFFFFF
+            or not 1 <= gap <= 0xFFFF or pow(omega, n, p) != 1 % p
+            or any(n % q == 0 for q in range(3, int(n ** 0.5) + 1, 2))):
+        raise ValueError("necklace preconditions not met (perm_modp_cuda.cu:955-968)")
+    depth, threads, per_sm = NECKLACE_CONFIG[m]
+    if m not in _frontiers:
+        _frontiers[m] = necklace_frontier(m, depth)
+    tasks_h = _frontiers[m]
+    g = _smallest_primitive_root_prime(n)
+    base, e = [], 1
+    for _ in range(m):
+        base.append(pow(omega, e, p))
+        e = e * g % n
+    base_sum = sum(base) % p
+    tasks = torch.from_numpy(tasks_h.view(np.uint8)).cuda()
+    dbase = torch.from_numpy(np.array(base, dtype=np.uint32).view(np.int32)).cuda()
+    counter = torch.zeros(1, dtype=torch.int32, device="cuda")
+    raw = torch.zeros(1, dtype=torch.int64, device="cuda")
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    d = driver()
+    f = d.function("modp", k_necklace(m, depth))
+    s = _stream(stream)
+    if timer:
+        timer.start(stream)
+    d.launch(f, sms * per_sm, threads, threads * 4, s,
+             [_ptr(tasks), ctypes.c_uint32(len(tasks_h)), _ptr(dbase), ctypes.c_uint32(base_sum),
+              ctypes.c_uint32(p), ctypes.c_uint32(gap), _ptr(counter), _ptr(raw)])
+    if timer:
+        timer.stop(stream)
+    r = (int(raw.cpu().item()) & ((1 << 64) - 1)) % p
+    minor = r * pow((p >> 1) + 1, m, p) % p                   # :1092-1097
+    return minor * (n % p) % p
+
+
+def schur_gpu_primes(n: int):
+    """perm_cuda.py:289-303, 372-404 (_plan_schur_crt_primes): descending odd
+    primes q == 1 (mod n) below 2^32 until their product times the
+    Graham-Lehmer modulus covers 2 * bound + 1."""
+    sys.path.insert(0, str(HERE.parent / "rivin-perm_gb300"))
+    from permgpu.crt import graham_lehmer_congruence, is_prime, schur_permanent_bound
+    target = 2 * schur_permanent_bound(n) + 1
+    cong = graham_lehmer_congruence(n)
+    prod = cong[1] if cong else 1
+    largest = (1 << 32) - 1
+    c = largest - ((largest - 1) % n)
+    if n % 2 == 1 and c % 2 == 0:
+        c -= n
+    step = n if n % 2 == 0 else 2 * n
+    primes = []
+    while prod < target and c >= 2:
+        if is_prime(c):
+            primes.append(c)
+            prod *= c
+        c -= step
+    return primes, cong
+
+
 # --- perm_binary_cuda.cu ---------------------------------------------------
 
 B_MAX_ORDER = 63                                    # perm_binary_cuda.cu:31-35
@@ -509,7 +623,7 @@ def main(argv=None):
     import time
     import torch
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workloads", default="generic24,generic32,grid40,binary40,float28")
+    ap.add_argument("--workloads", default="generic24,generic32,schur41,grid40,binary40,float28")
     ap.add_argument("--f64-sample", type=int, default=4)
     args = ap.parse_args(argv)
     root = HERE.parent
@@ -547,6 +661,30 @@ def main(argv=None):
             line(workload=wl, reference_kernel=kind, primes=len(primes), prime_bits=primes[0].bit_length(),
                  device_ms_per_prime=t.ms, device_s_total=sum(t.ms) / 1e3, wall_s=wall,
                  exact_result_matches=got == want)
+    if "schur41" in todo:
+        from permgpu.crt import crt, nth_root_of_unity, schur_permanent_bound
+        n = 41
+        want = int(json.loads((root / "tests" / "golden" / "schur.json").read_text())["table"][str(n)])
+        primes, cong = schur_gpu_primes(n)
+        t = Timer()
+        t0 = time.perf_counter()
+        res, ok = [], True
+        for q in primes:
+            w = nth_root_of_unity(n, q)
+            r = schur_necklace_modp(n, w, q, stream, t)
+            ok &= r == _lib.schur_residues(n, [q], [w])[0]
+            res.append(r)
+        wall = time.perf_counter() - t0
+        mods = primes + ([cong[1]] if cong else [])
+        rs = res + ([cong[0]] if cong else [])
+        x, mm = crt(rs, mods), 1
+        for q in mods:
+            mm *= q
+        got = x - mm if x > schur_permanent_bound(n) else x
+        line(workload="schur41", reference_kernel="schur_necklace_pm32_kernel<40,24> "
+             "(schur_permanent_modp_cuda)", primes=len(primes), device_ms_per_prime=t.ms,
+             device_s_total=sum(t.ms) / 1e3, wall_s=wall, residues_match=ok,
+             exact_result_matches=got == want)
     bins = {}
     if "grid40" in todo:
         import json as _j

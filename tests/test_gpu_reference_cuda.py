@@ -63,3 +63,15 @@ def test_fp64_glynn_kernel_values(lib, n):
     ref = ref_cuda.parallel_real(a)
     per, _, abs_sum = lib.glynn_f64_fwd_bwd(a[None], want_grad=False)
     assert abs(ref - per[0]) <= 1e-12 * abs_sum[0]
+
+
+def test_necklace_kernel_residue_s41(lib):
+    # the reference's persistent necklace kernel (M = 40, prefix depth 24),
+    # one of the three 2^32 - c primes its planner takes for perm(S_41);
+    # about 6 s of GPU time
+    from permgpu.crt import nth_root_of_unity
+    primes, _ = ref_cuda.schur_gpu_primes(41)
+    assert len(primes) == 3
+    q = primes[0]
+    w = nth_root_of_unity(41, q)
+    assert ref_cuda.schur_necklace_modp(41, w, q) == lib.schur_residues(41, [q], [w])[0]
