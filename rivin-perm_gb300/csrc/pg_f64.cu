@@ -79,7 +79,16 @@ __global__ void __launch_bounds__(128) glynn_f64_kernel(F64Args a) {
     double *slot = a.slots + (size_t)gw * f64_slot_doubles(N);
     double fsum = 0.0, fcomp = 0.0, fabs_sum = 0.0;
     double gabs = 0.0;
-    df G[N];
+    // Gradient columns by sign period: j < M change sign inside a chunk (V,
+    // compile-time signs), M <= j < lb (lb = log_block) keep one sign per
+    // chunk (GM[j - M] += +-W at each chunk's end), and j >= lb keep one sign
+    // per exact-initialisation block (one block sum WB, signed at the flush;
+    // the last column's sign is fixed).  Keeping per-column accumulators only
+    // for j < lb frees registers and most chunk-end adds.
+    constexpr int LBMAX = 12;                       // the host's largest log_block
+    constexpr int NMID = (N - 1 < LBMAX ? N - 1 : LBMAX) - M > 0
+                             ? (N - 1 < LBMAX ? N - 1 : LBMAX) - M : 1;
+    df GL[M > 0 ? M : 1], GM[NMID], WB;
     const int log_block = a.log_block < (N - 1) ? a.log_block : (N - 1);
     const uint64_t block_len = 1ull << log_block;
     const int mm = M < log_block ? M : log_block;   // chunk = 2^mm states
@@ -100,7 +109,10 @@ __global__ void __launch_bounds__(128) glynn_f64_kernel(F64Args a) {
             s = live ? df_from(v) : df{1.f, 0.f};
         }
 #pragma unroll
-        for (int j = 0; j < N; j++) G[j] = df{0.f, 0.f};
+        for (int t = 0; t < (M > 0 ? M : 1); t++) GL[t] = df{0.f, 0.f};
+#pragma unroll
+        for (int t = 0; t < NMID; t++) GM[t] = df{0.f, 0.f};
+        WB = df{0.f, 0.f};
         df fblk = df{0.f, 0.f};
         float fabs_blk = 0.f, gabs_blk = 0.f;
         for (uint64_t c0 = g0; c0 < g0 + block_len; c0 += (1ull << mm)) {
@@ -161,26 +173,42 @@ __global__ void __launch_bounds__(128) glynn_f64_kernel(F64Args a) {
             if (GRAD) {
                 const uint64_t gc = c0 ^ (c0 >> 1);
 #pragma unroll
-                for (int j = 0; j < N; j++) {
-                    if (j < M) {
-                        // column M-1 also depends on bit M of the chunk start
-                        const bool flip = (j == M - 1) && ((c0 >> M) & 1);
-                        G[j] = df_add(G[j], flip ? df_neg(V[j]) : V[j]);
-                    } else {
-                        const bool neg = j < N - 1 && ((gc >> j) & 1);
-                        G[j] = df_add(G[j], neg ? df_neg(W) : W);
+                for (int j = 0; j < M; j++) {
+                    // column M-1 also depends on bit M of the chunk start
+                    const bool flip = (j == M - 1) && ((c0 >> M) & 1);
+                    GL[j] = df_add(GL[j], flip ? df_neg(V[j]) : V[j]);
+                }
+#pragma unroll
+                for (int t = 0; t < NMID; t++) {
+                    const int j = M + t;
+                    if (j < N - 1 && j < log_block) {
+                        const bool neg = (gc >> j) & 1;
+                        GM[t] = df_add(GM[t], neg ? df_neg(W) : W);
                     }
                 }
+                WB = df_add(WB, W);
             }
         }
         kahan(fsum, fcomp, df_to(fblk));
         fabs_sum += (double)fabs_blk;
         gabs += (double)gabs_blk;
         if (GRAD && live) {
+            // columns j >= log_block: the block's one sign (gray bit j of the
+            // block start; the last column +)
+            const uint64_t gb = g0 ^ (g0 >> 1);
+            const double wb = df_to(WB);
 #pragma unroll
             for (int j = 0; j < N; j++) {
+                double v;
+                if (j < M) {
+                    v = df_to(GL[j]);
+                } else if (j - M < NMID && j < N - 1 && j < log_block) {
+                    v = df_to(GM[j - M < NMID ? j - M : 0]);
+                } else {
+                    v = (j < N - 1 && ((gb >> j) & 1)) ? -wb : wb;
+                }
                 double sm = slot[4 + lane * N + j], cp = slot[4 + N * N + lane * N + j];
-                kahan(sm, cp, df_to(G[j]));
+                kahan(sm, cp, v);
                 slot[4 + lane * N + j] = sm;
                 slot[4 + N * N + lane * N + j] = cp;
             }
