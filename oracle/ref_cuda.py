@@ -623,7 +623,7 @@ def main(argv=None):
     import time
     import torch
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workloads", default="generic24,generic32,schur41,grid40,binary40,float28")
+    ap.add_argument("--workloads", default="generic24,generic32,batch4096,schur41,grid40,binary40,float28")
     ap.add_argument("--f64-sample", type=int, default=4)
     args = ap.parse_args(argv)
     root = HERE.parent
@@ -661,6 +661,31 @@ def main(argv=None):
             line(workload=wl, reference_kernel=kind, primes=len(primes), prime_bits=primes[0].bit_length(),
                  device_ms_per_prime=t.ms, device_s_total=sum(t.ms) / 1e3, wall_s=wall,
                  exact_result_matches=got == want)
+    if "batch4096" in todo:
+        # the reference's own per-matrix GPU loop (one call per matrix and CRT
+        # prime, perm.py:1116-1127 primes) estimated from one matrix of each
+        # order: per-order time x the batch's count of that order
+        mats = workloads.batch4096()
+        by_order = {}
+        for m in mats:
+            by_order.setdefault(m.shape[0], []).append(m)
+        for kind, fn in (("ryser_modp (permanent_modp_cuda)", permanent_modp),
+                         ("glynn_modp (permanent_glynn_modp_kernel)", glynn_modp)):
+            est, ok, sample_s = 0.0, True, 0.0
+            for n, group in sorted(by_order.items()):
+                a = group[0]
+                bound = matrix_permanent_bound(a.tolist())
+                primes = _reference_primes(bound)
+                t = Timer()
+                res = [fn(a, q, stream, t) for q in primes]
+                ok &= signed_lift(res, primes, bound) == _lib.exact_permanent(a, _lib.exact_limbs(a))
+                dt = sum(t.ms) / 1e3
+                sample_s += dt
+                est += dt * len(group)
+            line(workload="batch4096", reference_kernel=kind,
+                 estimate="one matrix of each order 12..28 timed (all its primes), "
+                          "times the batch's count of that order",
+                 sample_device_s=sample_s, est_device_s_for_batch=est, exact_results_match=ok)
     if "schur41" in todo:
         from permgpu.crt import crt, nth_root_of_unity, schur_permanent_bound
         n = 41
