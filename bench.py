@@ -307,6 +307,9 @@ def run_reference(args, world, rank):
         "scaling": "weak", "vs_baseline": None, "dtype": "int64", "data": "synthetic",
         "config": {"workload": f"{args.workload}: {desc}", "n": n, "crt_primes": k_ref},
         "time_to_exact_s": (1 << (n - 1)) / value,
+        # CRT bits per second, K bits(p) 2^(n-1) / t over the K primes of
+        # the exact result: bits(p) times one prime's states per second
+        "crt_bits_per_s": p.bit_length() * per_prime,
         "cpu_baseline": {"value": value, "unit": "steps/s", "cores": threads,
                          "kind": "port", "sample": sample, "host": host_info()},
         "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0,
@@ -319,6 +322,7 @@ def run_gpu(args, world, rank, local):
     import numpy as np
     import torch
     from permgpu import _lib, workloads
+    from permgpu.crt import matrix_permanent_bound
 
     if not _lib.cuda_available():
         raise SystemExit("CUDA device not usable: the GPU path has no CPU fallback")
@@ -450,6 +454,9 @@ def run_gpu(args, world, rank, local):
                        "group_size": plan.group, "product_words": plan.words,
                        "l2": "flushed between timed steps (256 MiB write); inputs ~4 KiB"},
             "time_to_exact_s": step_ms * 1e-3,
+            # the same unit as a CRT walk's K bits(p) 2^(n-1) / t: the bits of
+            # the signed range the exact result covers, times states per second
+            "result_bits_per_s": (2 * matrix_permanent_bound(a.tolist()) + 1).bit_length() * value,
             "result_checked_against_reference": golden is not None,
             "roofline": {"bound": "imad", "achieved": achieved / 1e12, "peak": peak_lo / 1e12,
                          "unit": "Tops/s", "frac": achieved / peak_lo, "traffic": traffic,
