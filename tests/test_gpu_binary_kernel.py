@@ -77,6 +77,23 @@ def test_five_planes_and_two_tracking_words_order_48(lib):
         assert 2 * v == w
 
 
+def test_windows_on_and_off_the_group_grid(lib):
+    # a window whose first chunk is a multiple of 32 runs the split
+    # evaluation with chunk groups taken from a counter; one that starts
+    # three chunks later runs without the split, dealt round-robin; both
+    # against the general kernel's windows on the row-doubled matrix
+    from permgpu import shard
+    a = (np.random.default_rng(411).random((40, 40)) < 0.5).astype(np.int64)
+    assert _planes(lib, a) >= 2
+    b = a.copy()
+    b[0] *= 2
+    for lo in (1 << 30, (1 << 30) + 3 * (1 << 10), (1 << 38) + 5 * (1 << 10)):
+        hi = lo + (1 << 22) + 7 * (1 << 10)
+        v = shard.words_value(shard.exact_partial_words(a, lo, hi))
+        w = shard.words_value(shard.exact_partial_words(b, lo, hi))
+        assert 2 * v == w
+
+
 def test_zero_rows_permutations_and_ones(lib):
     n = 26
     rng = np.random.default_rng(26)
